@@ -1,0 +1,482 @@
+// TEST INFRASTRUCTURE — CPU oracle for the SimpleWindErosion hot path.
+//
+// Part 1 restates the reference's sequential algorithm on SoA float maps,
+// operation by operation (every float op in the reference's order, with the
+// vector arithmetic of oracle/glm_shim.hpp):
+//   so_erode      <- World::erode          source/world.hpp:36-77
+//   fly<>         <- Wind::fly             source/wind.hpp:28-117
+//   cascade       <- World::cascade        source/world.hpp:79-153
+//   normal        <- quad::_normal         source/cellpool.h:200-223
+//   oob / index   <- map::oob, math::flatten  cellpool.h:432-438, math.h:11-14
+// rand() argument order: g++ (x86-64, -O2) evaluates the constructor
+// arguments of ivec2(rand(),rand()), vec2(rand(),rand()) and
+// vec3(rand(),rand(),rand()) right to left, so the first call of each group
+// feeds the last component (probed by ref_probe_order in ref_harness.cpp and
+// pinned by the bitwise oracle-vs-reference tests).
+//
+// Part 2 is a CPU model of the library's parallel fixed-point mode, written
+// so that every float operation matches the CUDA kernel (compiled with
+// -fmad=false, explicit fmaf only) bit for bit.
+//
+// Only tests, the smoke check and the bench's CPU legs load this file.
+#include "swe_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+struct V3 {
+  float x, y, z;
+};
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 mulv(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline V3 smul(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+inline V3 muls(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline V3 divs(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+inline V3 subs(V3 a, float s) { return v3(a.x - s, a.y - s, a.z - s); }
+inline float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline float length(V3 v) { return std::sqrt(dot(v, v)); }
+inline V3 normalize(V3 v) { return muls(v, 1.0f / std::sqrt(dot(v, v))); }
+inline V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+inline V3 mix(V3 x, V3 y, float a) { return add(muls(x, 1.0f - a), muls(y, a)); }
+
+// ---------------------------------------------------------------- glibc rand
+// The C library's rand() (TYPE_3 additive feedback generator): seed r[0],
+// r[i] = 16807 r[i-1] mod (2^31-1) for i < 31, r[i] = r[i-31] for i in
+// 31..33, then r[i] = r[i-31] + r[i-3] (mod 2^32); output i-344 is r[i] >> 1.
+struct GlibcRand {
+  uint32_t r[34];
+  int pos;
+  void seed(uint32_t s) {
+    int32_t w = (int32_t)(s == 0 ? 1u : s);
+    int32_t t[31];
+    t[0] = w;
+    for (int i = 1; i < 31; i++) {
+      int64_t v = (16807LL * (int64_t)t[i - 1]) % 2147483647LL;
+      if (v < 0) v += 2147483647LL;
+      t[i] = (int32_t)v;
+    }
+    for (int i = 0; i < 31; i++) r[i] = (uint32_t)t[i];
+    for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+    pos = 0;  // r holds indices 0..33; next index to produce is 34
+    base = 34;
+    for (int i = 0; i < 310; i++) next_raw();
+  }
+  long base;
+  uint32_t next_raw() {
+    // ring of 34: index i lives at slot i % 34
+    long i = base;
+    uint32_t v = r[(i - 31) % 34] + r[(i - 3) % 34];
+    r[i % 34] = v;
+    base = i + 1;
+    return v;
+  }
+  int next() { return (int)(next_raw() >> 1); }
+};
+
+// ---------------------------------------------------------------- exp kinds
+inline float exp_libm(float x) { return std::exp(x); }        // glibc expf, as the reference
+inline float exp_cr(float x) { return (float)std::exp((double)x); }  // correctly rounded
+
+}  // namespace
+
+// Own single-precision exp for the parallel mode: Cody-Waite reduction
+// x = k ln2 + r, Taylor polynomial of degree 7 for e^r on |r| <= ln2/2 in
+// Horner form with fused multiply-adds, scaling by 2^k through the exponent
+// field. Results below e^-86 flush to 0. Identical on CPU and GPU because it
+// uses only correctly rounded IEEE operations.
+extern "C" float so_expf_poly(float x) {
+  if (!(x == x)) return x;
+  if (x < -86.0f) return 0.0f;
+  if (x > 88.0f) return HUGE_VALF;
+  float k = std::rint(x * 1.44269504f);
+  float r = std::fmaf(k, -0.693145752f, x);
+  r = std::fmaf(k, -1.42860677e-6f, r);
+  float p = 1.98412698e-4f;
+  p = std::fmaf(p, r, 1.38888889e-3f);
+  p = std::fmaf(p, r, 8.33333333e-3f);
+  p = std::fmaf(p, r, 4.16666667e-2f);
+  p = std::fmaf(p, r, 1.66666667e-1f);
+  p = std::fmaf(p, r, 0.5f);
+  p = std::fmaf(p, r, 1.0f);
+  p = std::fmaf(p, r, 1.0f);
+  int ki = (int)k;
+  uint32_t bits = (uint32_t)(ki + 127) << 23;
+  float scale;
+  std::memcpy(&scale, &bits, 4);
+  return p * scale;
+}
+
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the
+// multiply-xor round function with the paper's multipliers and Weyl key
+// increments.
+extern "C" void so_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                              uint32_t k1, uint32_t* out) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int round = 0; round < 10; round++) {
+    uint64_t p0 = (uint64_t)M0 * c0;
+    uint64_t p1 = (uint64_t)M1 * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n1 = lo1;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    uint32_t n3 = lo0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += W0; k1 += W1;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+struct so_world {
+  int nx, nz;
+  so_params p;
+  std::vector<float> f[9];  // height, massflow, momx, momy, momz, 4 tracks (cellpool.h:226-240)
+  int rng = SO_RNG_GLIBC;
+  GlibcRand grand;
+  const int32_t* tape = nullptr;
+  long tape_len = 0, tape_pos = 0;
+  int exp_kind = SO_EXP_LIBM;
+  int64_t st_steps = 0, st_particles = 0, st_transfers = 0;
+  // parallel model state
+  std::vector<int32_t> hq;
+  bool hq_valid = false;
+  int64_t exported_q = 0;
+
+  int rnd() {
+    switch (rng) {
+      case SO_RNG_LIBC: return std::rand();
+      case SO_RNG_GLIBC: return grand.next();
+      default: return tape_pos < tape_len ? tape[tape_pos++] : 0;
+    }
+  }
+  float ex(float x) const { return exp_kind == SO_EXP_CR ? exp_cr(x) : exp_libm(x); }
+  bool oob(int x, int z) const { return x < 0 || z < 0 || x >= nx || z >= nz; }
+  long idx(int x, int z) const { return (long)x * nz + z; }
+  float h(int x, int z) const { return oob(x, z) ? 0.0f : f[0][idx(x, z)]; }
+};
+
+namespace {
+
+// quad::_normal (cellpool.h:200-223) over a height accessor.
+template <class H>
+V3 normal_at(const so_world* w, int x, int z, H height) {
+  V3 n = v3(0, 0, 0);
+  const V3 s = v3(1.0f, w->p.mapscale, 1.0f);
+  const float hp = height(x, z);
+  if (!w->oob(x + 1, z + 1))
+    n = add(n, cross(mulv(s, v3(0.0f, height(x, z + 1) - hp, 1.0f)),
+                     mulv(s, v3(1.0f, height(x + 1, z) - hp, 0.0f))));
+  if (!w->oob(x - 1, z - 1))
+    n = add(n, cross(mulv(s, v3(0.0f, height(x, z - 1) - hp, -1.0f)),
+                     mulv(s, v3(-1.0f, height(x - 1, z) - hp, 0.0f))));
+  if (!w->oob(x + 1, z - 1))
+    n = add(n, cross(mulv(s, v3(1.0f, height(x + 1, z) - hp, 0.0f)),
+                     mulv(s, v3(0.0f, height(x, z - 1) - hp, -1.0f))));
+  if (!w->oob(x - 1, z + 1))
+    n = add(n, cross(mulv(s, v3(-1.0f, height(x - 1, z) - hp, 0.0f)),
+                     mulv(s, v3(0.0f, height(x, z + 1) - hp, 1.0f))));
+  if (length(n) > 0) n = normalize(n);
+  return n;
+}
+
+const int NB_DX[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+const int NB_DZ[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+
+struct Nb {
+  int x, z;
+  float h, d;
+};
+
+// libstdc++ std::sort on <= 16 elements is this insertion sort; with the
+// strict comparator a.h > b.h it is stable.
+template <class T, class Gt>
+void insertion_sort_desc(T* a, int n, Gt gt) {
+  for (int i = 1; i < n; i++) {
+    T val = a[i];
+    if (gt(val, a[0])) {
+      for (int j = i; j > 0; j--) a[j] = a[j - 1];
+      a[0] = val;
+    } else {
+      int j = i;
+      while (gt(val, a[j - 1])) {
+        a[j] = a[j - 1];
+        j--;
+      }
+      a[j] = val;
+    }
+  }
+}
+
+// World::cascade (world.hpp:79-153).
+void cascade(so_world* w, int x, int z) {
+  Nb sn[8];
+  int num = 0;
+  for (int k = 0; k < 8; k++) {
+    int nx_ = x + NB_DX[k], nz_ = z + NB_DZ[k];
+    if (w->oob(nx_, nz_)) continue;
+    float dx = (float)NB_DX[k], dz = (float)NB_DZ[k];
+    sn[num++] = Nb{nx_, nz_, w->f[0][w->idx(nx_, nz_)], std::sqrt(dx * dx + dz * dz)};
+  }
+  insertion_sort_desc(sn, num, [](const Nb& a, const Nb& b) { return a.h > b.h; });
+  float* H = w->f[0].data();
+  const long c = w->idx(x, z);
+  for (int i = 0; i < num; i++) {
+    float diff = H[c] - sn[i].h;
+    if (diff == 0) continue;
+    float excess = std::fabs(diff) - sn[i].d * w->p.maxdiff;
+    if (excess <= 0) continue;
+    float transfer = w->p.settling * excess / 2.0f;
+    const long q = w->idx(sn[i].x, sn[i].z);
+    if (diff > 0) {
+      H[c] -= transfer;
+      H[q] += transfer;
+    } else {
+      H[c] += transfer;
+      H[q] -= transfer;
+    }
+    w->st_transfers++;
+  }
+}
+
+struct Particle {
+  int age;
+  float sediment;
+  V3 pos, speed, pspeed;
+};
+
+// Wind::fly (wind.hpp:28-117). Frozen = no writes to the map.
+template <bool Frozen>
+bool fly(so_world* w, Particle& P) {
+  const int ix = (int)std::round(P.pos.x);
+  const int iz = (int)std::round(P.pos.z);
+  if (w->oob(ix, iz)) return false;
+  const V3 n = normal_at(w, ix, iz, [w](int a, int b) { return w->h(a, b); });
+  const long c = w->idx(ix, iz);
+  float* H = w->f[0].data();
+  if (P.age == 0 || P.pos.y < H[c]) P.pos.y = H[c];
+  if (P.age++ > w->p.max_age) return false;
+
+  float hfac = w->ex(-(P.pos.y - H[c]) / w->p.boundarylayer);
+  if (hfac < 0) hfac = 0;
+
+  float shadow = dot(normalize(P.pspeed), n);
+  if (shadow < 0) shadow = 0;
+  shadow = 1.0f - shadow;
+  P.speed = add(P.speed, smul(0.05f, sub(smul(0.1f + 0.9f * shadow, P.pspeed), P.speed)));
+
+  if (P.pos.y > H[c]) P.speed.y -= w->p.gravity * P.sediment;
+
+  float collision = -dot(normalize(P.speed), n);
+  if (collision < 0) collision = 0;
+
+  V3 rspeed = cross(n, cross(smul(1.0f - collision, P.speed), n));
+  P.speed = add(P.speed,
+                smul(0.9f, sub(smul(shadow, mix(P.pspeed, rspeed, shadow * hfac)), P.speed)));
+
+  // vec3(rand()%1001, rand()%1001, rand()%1001): first call -> z (see header)
+  const int rz = w->rnd() % 1001;
+  const int ry = w->rnd() % 1001;
+  const int rx = w->rnd() % 1001;
+  P.speed = add(P.speed,
+                divs(smul(0.1f * hfac * collision, subs(v3((float)rx, (float)ry, (float)rz), 500.0f)),
+                     500.0f));
+
+  const float drag = (float)(1.0f - 0.3 * (double)P.sediment);
+  P.speed = v3(P.speed.x * drag, P.speed.y * drag, P.speed.z * drag);
+
+  P.pos = add(P.pos, P.speed);
+
+  if (!Frozen) {
+    w->f[6][c] += P.speed.x;
+    w->f[7][c] += P.speed.y;
+    w->f[8][c] += P.speed.z;
+    w->f[5][c] += P.sediment;
+  }
+
+  float force = -dot(normalize(P.speed), n) * length(P.speed);
+  if (force < 0) force = 0;
+  float lift = (1.0f - collision) * length(P.speed);
+  float capacity = force * hfac + 0.02f * lift * hfac;
+
+  float diff = capacity - P.sediment;
+  if (!Frozen) H[c] -= w->p.suspension * diff;
+  P.sediment += w->p.suspension * diff;
+
+  if (!Frozen) cascade(w, ix, iz);
+  return true;
+}
+
+void record(const Particle& P, bool alive, float* rec) {
+  rec[0] = alive ? 1.0f : 0.0f;
+  rec[1] = (float)P.age;
+  rec[2] = P.pos.x; rec[3] = P.pos.y; rec[4] = P.pos.z;
+  rec[5] = P.speed.x; rec[6] = P.speed.y; rec[7] = P.speed.z;
+  rec[8] = P.sediment;
+}
+
+Particle spawn_at(const so_world* w, float x, float z) {
+  Particle P;
+  P.age = 0;
+  P.sediment = 0.0f;
+  P.pos = v3(x, 0.0f, z);
+  P.speed = v3(0, 0, 0);
+  P.pspeed = v3(w->p.pspeed[0], w->p.pspeed[1], w->p.pspeed[2]);
+  return P;
+}
+
+}  // namespace
+
+extern "C" {
+
+void so_params_default(so_params* p) {
+  p->max_age = 512;
+  p->boundarylayer = 2.0f;
+  p->suspension = 0.05f;
+  p->gravity = 0.1f;
+  p->lrate = 0.1f;
+  p->maxdiff = 0.005f;
+  p->settling = 1.0f;
+  p->mapscale = 80.0f;
+  p->pspeed[0] = 1.0f; p->pspeed[1] = 0.0f; p->pspeed[2] = 0.0f;
+  p->frac_bits = 24;
+}
+
+so_world* so_create(int nx, int nz, const so_params* p) {
+  so_world* w = new so_world();
+  w->nx = nx;
+  w->nz = nz;
+  if (p) w->p = *p; else so_params_default(&w->p);
+  for (auto& v : w->f) v.assign((size_t)nx * nz, 0.0f);
+  w->grand.seed(1);
+  return w;
+}
+
+void so_destroy(so_world* w) { delete w; }
+void so_set_params(so_world* w, const so_params* p) { w->p = *p; }
+
+void so_set_field(so_world* w, int field, const float* src) {
+  std::memcpy(w->f[field].data(), src, sizeof(float) * w->f[field].size());
+  if (field == 0) w->hq_valid = false;
+}
+
+void so_get_field(so_world* w, int field, float* dst) {
+  std::memcpy(dst, w->f[field].data(), sizeof(float) * w->f[field].size());
+}
+
+void so_set_rng(so_world* w, int rng, uint32_t seed) {
+  w->rng = rng;
+  if (rng == SO_RNG_GLIBC) w->grand.seed(seed);
+  if (rng == SO_RNG_LIBC) std::srand(seed);
+}
+void so_set_exp(so_world* w, int exp_kind) { w->exp_kind = exp_kind; }
+void so_set_tape(so_world* w, const int32_t* tape, long n) {
+  w->tape = tape; w->tape_len = n; w->tape_pos = 0; w->rng = SO_RNG_TAPE;
+}
+long so_tape_pos(so_world* w) { return w->tape_pos; }
+
+void so_stats(so_world* w, int64_t* steps, int64_t* particles, int64_t* transfers) {
+  *steps = w->st_steps; *particles = w->st_particles; *transfers = w->st_transfers;
+}
+
+// World::erode(P), `cycles` times (world.hpp:36-77).
+void so_erode(so_world* w, int particles, int cycles) {
+  w->st_steps = w->st_particles = w->st_transfers = 0;
+  const size_t n = (size_t)w->nx * w->nz;
+  const float lrate = w->p.lrate;
+  for (int cyc = 0; cyc < cycles; cyc++) {
+    for (int k = 5; k < 9; k++) std::fill(w->f[k].begin(), w->f[k].end(), 0.0f);
+    for (int i = 0; i < particles; i++) {
+      // ivec2(rand()%res.x, rand()%res.y): first call -> z
+      const int z = w->rnd() % w->nz;
+      const int x = w->rnd() % w->nx;
+      // vec2(rand()%1000, rand()%1000)/1000: first call -> z
+      const int fz = w->rnd() % 1000;
+      const int fx = w->rnd() % 1000;
+      const float px = (float)x + (float)fx / 1000.0f;
+      const float pz = (float)z + (float)fz / 1000.0f;
+      Particle P = spawn_at(w, px, pz);
+      w->st_particles++;
+      while (fly<false>(w, P)) w->st_steps++;
+    }
+    float* m = w->f[1].data();
+    float* mx = w->f[2].data();
+    float* my = w->f[3].data();
+    float* mz = w->f[4].data();
+    const float* tm = w->f[5].data();
+    const float* tx = w->f[6].data();
+    const float* ty = w->f[7].data();
+    const float* tz = w->f[8].data();
+    for (size_t i = 0; i < n; i++) {
+      m[i] = (1.0f - lrate) * m[i] + lrate * tm[i];
+      mx[i] = (1.0f - lrate) * mx[i] + lrate * tx[i];
+      my[i] = (1.0f - lrate) * my[i] + lrate * ty[i];
+      mz[i] = (1.0f - lrate) * mz[i] + lrate * tz[i];
+    }
+  }
+  w->hq_valid = false;
+}
+
+void so_normal(so_world* w, int x, int z, float* out3) {
+  V3 n = normal_at(w, x, z, [w](int a, int b) { return w->h(a, b); });
+  out3[0] = n.x; out3[1] = n.y; out3[2] = n.z;
+}
+
+void so_cascade(so_world* w, int x, int z) {
+  cascade(w, x, z);
+  w->hq_valid = false;
+}
+
+int so_trace(so_world* w, int n, const float* spawn_xz, int steps, const int32_t* tape, float* out) {
+  const int saved_rng = w->rng;
+  for (int p = 0; p < n; p++) {
+    Particle P = spawn_at(w, spawn_xz[2 * p], spawn_xz[2 * p + 1]);
+    bool alive = true;
+    for (int s = 0; s < steps; s++) {
+      float* rec = out + ((long)p * steps + s) * 9;
+      if (alive) {
+        w->tape = tape + ((long)p * steps + s) * 3;
+        w->tape_len = 3; w->tape_pos = 0; w->rng = SO_RNG_TAPE;
+        alive = fly<true>(w, P);
+      }
+      record(P, alive, rec);
+    }
+  }
+  w->rng = saved_rng;
+  return 0;
+}
+
+int so_fly_live(so_world* w, float x, float z, int steps, const int32_t* tape, float* out) {
+  const int saved_rng = w->rng;
+  Particle P = spawn_at(w, x, z);
+  bool alive = true;
+  int ok = 0;
+  for (int s = 0; s < steps; s++) {
+    if (alive) {
+      if (tape) { w->tape = tape + (long)s * 3; w->tape_len = 3; w->tape_pos = 0; w->rng = SO_RNG_TAPE; }
+      alive = fly<false>(w, P);
+      w->rng = saved_rng;
+      if (alive) ok++;
+    }
+    if (out) record(P, alive, out + (long)s * 9);
+  }
+  w->hq_valid = false;
+  return ok;
+}
+
+void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out) {
+  GlibcRand g;
+  g.seed(seed);
+  for (int i = 0; i < n; i++) out[i] = g.next();
+}
+
+}  // extern "C"
