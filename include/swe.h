@@ -1,0 +1,178 @@
+/*
+ * swe.h — C ABI of the GB300 SimpleWindErosion hot path.
+ *
+ * Drop-in for the reference's static simulation API (source/world.hpp:9-24,
+ * source/wind.hpp:4-21): World::erode(int) and the World/Wind statics become
+ * a world object with device-resident cell maps. The reference has no FFI;
+ * each entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Return value: SWE_OK (0) or a negative SWE_ERR_* code; swe_last_error()
+ *    gives the message of the calling thread's last failure.
+ *  - Ownership: the caller owns host buffers; the library owns device memory.
+ *  - Threading: one world per host thread at a time; each world has its own
+ *    CUDA stream. Work is enqueued asynchronously; swe_world_sync(),
+ *    downloads and the ledger/statistics queries wait for it.
+ *  - Layout: every field is nx*nz floats, row-major [x][z] with z contiguous,
+ *    index x*nz + z (math::flatten, source/include/math.h:11-14).
+ *  - No entry point falls back to the CPU: without a usable CUDA device,
+ *    swe_world_create fails with SWE_ERR_CUDA.
+ */
+#ifndef SWE_H
+#define SWE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWE_OK 0
+#define SWE_ERR_INVALID (-1)       /* bad argument or size                      */
+#define SWE_ERR_CUDA (-2)          /* CUDA runtime error                        */
+#define SWE_ERR_DEVICE (-3)        /* a kernel reported a problem in its status */
+#define SWE_ERR_NO_MEMORY (-4)     /* device allocation failed                  */
+
+/* Device status bits (swe_world_status). */
+#define SWE_STATUS_NONFINITE 0x1u  /* a particle produced NaN/Inf and was retired */
+#define SWE_STATUS_RANGE 0x2u      /* a fixed-point height left its safe range     */
+#define SWE_STATUS_TAPE 0x4u       /* an ordered-mode rand tape ran out            */
+
+/* Simulation constants; swe_params_default() gives the reference's values.
+ * Replaces the statics Wind::maxAge/boundarylayer/suspension/gravity
+ * (wind.hpp:15-26), World::lrate/maxdiff/settling (world.hpp:26-32),
+ * quad::mapscale (cellpool.h:184) and the per-particle prevailing wind
+ * Wind::pspeed (wind.hpp:13). */
+typedef struct swe_params {
+  int max_age;          /* 512   */
+  float boundarylayer;  /* 2.0   */
+  float suspension;     /* 0.05  */
+  float gravity;        /* 0.1   */
+  float lrate;          /* 0.1   */
+  float maxdiff;        /* 0.005 */
+  float settling;       /* 1.0   */
+  float mapscale;       /* 80    */
+  float pspeed[3];      /* (1,0,0) */
+  int frac_bits;        /* parallel mode: fixed-point fraction bits, 8..28 (24) */
+} swe_params;
+
+/* Per-cell fields, in the order of quad::cell (cellpool.h:226-240). */
+typedef enum swe_field {
+  SWE_HEIGHT = 0,
+  SWE_MASSFLOW = 1,
+  SWE_MOMENTUMX = 2,
+  SWE_MOMENTUMY = 3,
+  SWE_MOMENTUMZ = 4,
+  SWE_MASSFLOW_TRACK = 5,
+  SWE_MOMENTUMX_TRACK = 6,
+  SWE_MOMENTUMY_TRACK = 7,
+  SWE_MOMENTUMZ_TRACK = 8
+} swe_field;
+
+/* How World::erode's particles are run.
+ *  ORDERED:  particles one after another, exactly as the reference
+ *            (world.hpp:47-67), with the C library rand() sequence of
+ *            srand(seed) (or a caller tape). One GPU thread; a parity mode.
+ *  PARALLEL: all particles of a cycle fly together in lock-step steps. Each
+ *            step reads the height map as it was at the start of the step;
+ *            deposits, erosion and cascade transfers are added with integer
+ *            atomics in fixed point, so mass is conserved exactly and the
+ *            result does not depend on thread scheduling. Random numbers come
+ *            from a counter-based generator keyed by (seed, cycle, particle,
+ *            step). The throughput mode. */
+typedef enum swe_mode { SWE_MODE_ORDERED = 0, SWE_MODE_PARALLEL = 1 } swe_mode;
+
+typedef struct swe_world swe_world;
+
+/* The reference's constants (see swe_params). */
+void swe_params_default(swe_params* p);
+
+/* Allocate a world of nx*nz cells on the current CUDA device, all fields
+ * zero. Replaces mappool::pool::reserve + quad::map::init node setup
+ * (cellpool.h:121-164, 339-356) and srand(SEED) (SimpleWindErosion.cpp:27-34):
+ * `seed` seeds both the ordered-mode rand() replica and the parallel-mode
+ * generator. */
+int swe_world_create(int nx, int nz, const swe_params* p, uint64_t seed, swe_world** out);
+void swe_world_destroy(swe_world* w);
+int swe_world_set_params(swe_world* w, const swe_params* p);
+int swe_world_get_params(swe_world* w, swe_params* p);
+int swe_world_size(swe_world* w, int* nx, int* nz);
+
+/* Copy one field host -> device / device -> host (n must be nx*nz).
+ * Replaces direct cell access (cell->height etc., cellpool.h:226-240,
+ * SimpleWindErosion.cpp:224-230). Uploading SWE_HEIGHT resets the mass
+ * ledger. */
+int swe_world_upload(swe_world* w, swe_field f, const float* host, size_t n);
+int swe_world_download(swe_world* w, swe_field f, float* host, size_t n);
+
+/* Device address of a field (nx*nz floats), for zero-copy callers. Valid until
+ * swe_world_destroy; after a PARALLEL erode, SWE_HEIGHT holds the fixed-point
+ * map converted back to float. */
+int swe_world_device_field(swe_world* w, swe_field f, void** dev_ptr);
+
+/* World::erode(particles_per_cycle), `cycles` times (world.hpp:36-77):
+ * track reset, particle flights, EMA update of massflow/momentum. Asynchronous
+ * on the world's stream. */
+int swe_world_erode(swe_world* w, int cycles, int particles_per_cycle, swe_mode mode);
+
+/* Wait for the world's queued work; returns SWE_ERR_DEVICE if a kernel set a
+ * status bit since the last call (bits in *status if non-NULL, then cleared). */
+int swe_world_sync(swe_world* w);
+int swe_world_status(swe_world* w, uint32_t* status);
+
+/* Ordered mode random source. swe_world_seed_rand reseeds the rand() replica
+ * (srand, SimpleWindErosion.cpp:29/33). swe_world_set_rand_tape makes ordered
+ * erodes consume the given raw rand() values in call order instead (4 per
+ * spawn, world.hpp:52-54; 3 per successful step, wind.hpp:83); n = 0 returns
+ * to the replica. */
+int swe_world_seed_rand(swe_world* w, uint32_t seed);
+int swe_world_set_rand_tape(swe_world* w, const int32_t* tape, size_t n);
+
+/* Mass ledger of the parallel mode in fixed point (units of 2^-frac_bits):
+ * map_q = sum of heights, inflight_q = sediment carried by particles still
+ * flying (0 between erode calls), exported_q = sediment carried off the map
+ * or dropped at max_age since the last height upload. map_q + inflight_q +
+ * exported_q stays constant. */
+int swe_world_mass_ledger(swe_world* w, int64_t* map_q, int64_t* inflight_q, int64_t* exported_q);
+
+/* Counters of the last swe_world_erode call: successful fly steps, spawned
+ * particles, cascade transfers. */
+int swe_world_stats(swe_world* w, int64_t* particle_steps, int64_t* particles, int64_t* transfers);
+
+/* Frozen-map trajectories (Wind::fly, wind.hpp:28-117, with the map left
+ * unchanged). Particle p spawns at (spawn_xz[2p], spawn_xz[2p+1]); its step s
+ * draws turbulence from turb_tape[(p*steps+s)*3 + 0..2] (raw rand() values in
+ * call order). out_state gets 9 floats per (p, s): alive, age, pos.xyz,
+ * speed.xyz, sediment. */
+int swe_trace_particles(swe_world* w, const float* spawn_xz, int n, int steps,
+                        const int32_t* turb_tape, float* out_state);
+
+/* One particle flown on the live map for up to `steps` Wind::fly calls
+ * (ordered semantics, writes happen). turb_tape: 3 raw rand() values per
+ * step, or NULL to draw from the rand() replica. out_state as above (may be
+ * NULL). *ok_steps = successful fly calls. */
+int swe_world_fly(swe_world* w, float x, float z, int steps, const int32_t* turb_tape,
+                  float* out_state, int* ok_steps);
+
+/* World::cascade at one cell (world.hpp:79-153), on the float height map. */
+int swe_world_cascade_at(swe_world* w, int x, int z);
+
+/* Surface normal of every cell, quad::_normal (cellpool.h:200-223) as
+ * map::normal calls it (cellpool.h:478-480): 3*nx*nz floats (x,y,z per cell)
+ * written to host_out. */
+int swe_world_normals(swe_world* w, float* host_out, size_t n);
+
+/* The exponential the exact-semantics kernels use (the reference's
+ * std::exp(float), wind.hpp:50, i.e. this machine's C library expf,
+ * reproduced on the device) evaluated for the n float bit patterns
+ * first_bits, first_bits+1, ...; for checking it against the C library. */
+int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host_y);
+
+/* Message of the calling thread's last error ("" if none). */
+const char* swe_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWE_H */

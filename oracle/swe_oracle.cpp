@@ -480,3 +480,299 @@ void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Part 2: CPU model of the parallel fixed-point mode. Same definitions as the
+// CUDA kernels (simplewinderosion_gb300/csrc/swe_parallel.cu). One step:
+//   fly     every live particle runs Wind::fly against the heights as they
+//           were at the start of the step; its exchange with its cell goes
+//           into a delta map D and its cell's visit count into C (integers).
+//   cascade four passes over 32x32 tiles, tile colour (tx%2, tz%2). A tile
+//           works on its cells and a one-cell halo: heights + D; then for the
+//           nine cell colours (x%3, z%3) in order, every cell with C > 0
+//           runs World::cascade C times on the current heights; halo cells
+//           go back without their D, own cells absorb theirs.
+// Same-colour tiles and same-colour cells touch disjoint 3x3 neighbourhoods,
+// so each pass is free of conflicts and the order of the whole step is fixed.
+// ============================================================================
+namespace {
+
+constexpr int kTile = 32;
+
+int32_t to_fixed(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483648.0f) return INT32_MAX;
+  if (v < -2147483648.0f) return INT32_MIN;
+  return (int32_t)std::lrintf(v);
+}
+int64_t to_fixed64(float v) {
+  if (v != v) return 0;
+  if (v >= 9223372036854775808.0f) return INT64_MAX;
+  if (v < -9223372036854775808.0f) return INT64_MIN;
+  return (int64_t)std::llrintf(v);
+}
+inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+inline int32_t wsub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+
+struct PState {
+  int id, age, sed_q;
+  float px, py, pz, vx, vy, vz;
+};
+
+struct ParCtx {
+  so_world* w;
+  const int32_t* H;
+  int32_t* D;
+  int32_t* C;
+  int64_t* tq[4];
+  uint32_t seed_lo, seed_hi, c_lo, c_hi;
+  int64_t exported, steps, transfers;
+};
+
+// One step of one particle against the step-start heights; true if alive.
+bool par_fly(ParCtx& X, PState& P, int step) {
+  so_world* w = X.w;
+  const so_params& c = w->p;
+  const int nx = w->nx, nz = w->nz;
+  const float scale = (float)(1u << c.frac_bits);
+  const float inv = 1.0f / scale;
+  const float sed = (float)P.sed_q * inv;
+  const bool inrange = std::fabs(P.px) < 1073741824.0f && std::fabs(P.pz) < 1073741824.0f;
+  const int ix = inrange ? (int)std::round(P.px) : -1;
+  const int iz = inrange ? (int)std::round(P.pz) : -1;
+  if (ix < 0 || iz < 0 || ix >= nx || iz >= nz) return false;
+  const bool vx0 = ix > 0, vx2 = ix + 1 < nx, vz0 = iz > 0, vz2 = iz + 1 < nz;
+  const long ci = (long)ix * nz + iz;
+  const float h11 = (float)X.H[ci] * inv;
+  const float h01 = vx0 ? (float)X.H[ci - nz] * inv : 0.0f;
+  const float h21 = vx2 ? (float)X.H[ci + nz] * inv : 0.0f;
+  const float h10 = vz0 ? (float)X.H[ci - 1] * inv : 0.0f;
+  const float h12 = vz2 ? (float)X.H[ci + 1] * inv : 0.0f;
+  V3 n = v3(0.0f, 0.0f, 0.0f);
+  const V3 s = v3(1.0f, c.mapscale, 1.0f);
+  if (vx2 && vz2) n = add(n, cross(mulv(s, v3(0.0f, h12 - h11, 1.0f)), mulv(s, v3(1.0f, h21 - h11, 0.0f))));
+  if (vx0 && vz0) n = add(n, cross(mulv(s, v3(0.0f, h10 - h11, -1.0f)), mulv(s, v3(-1.0f, h01 - h11, 0.0f))));
+  if (vx2 && vz0) n = add(n, cross(mulv(s, v3(1.0f, h21 - h11, 0.0f)), mulv(s, v3(0.0f, h10 - h11, -1.0f))));
+  if (vx0 && vz2) n = add(n, cross(mulv(s, v3(-1.0f, h01 - h11, 0.0f)), mulv(s, v3(0.0f, h12 - h11, 1.0f))));
+  if (length(n) > 0.0f) n = normalize(n);
+
+  float py = P.py;
+  if (P.age == 0 || py < h11) py = h11;
+  P.py = py;
+  if (P.age++ > c.max_age) return false;
+  float hfac = so_expf_poly(-(py - h11) / c.boundarylayer);
+  if (hfac < 0.0f) hfac = 0.0f;
+  const V3 ps = v3(c.pspeed[0], c.pspeed[1], c.pspeed[2]);
+  V3 sp = v3(P.vx, P.vy, P.vz);
+  float shadow = dot(normalize(ps), n);
+  if (shadow < 0.0f) shadow = 0.0f;
+  shadow = 1.0f - shadow;
+  sp = add(sp, smul(0.05f, sub(smul(0.1f + 0.9f * shadow, ps), sp)));
+  if (py > h11) sp.y -= c.gravity * sed;
+  float collision = -dot(normalize(sp), n);
+  if (collision < 0.0f) collision = 0.0f;
+  const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
+  sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
+  uint32_t u[4];
+  so_philox4x32((uint32_t)P.id, (uint32_t)step, X.c_lo, X.c_hi, X.seed_lo, X.seed_hi, u);
+  const float rx = (float)(int)(u[0] % 1001u), ry = (float)(int)(u[1] % 1001u), rz = (float)(int)(u[2] % 1001u);
+  sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
+  const float drag = 1.0f - 0.3f * sed;
+  sp = v3(sp.x * drag, sp.y * drag, sp.z * drag);
+  const float px = P.px + sp.x, pz = P.pz + sp.z;
+  py = py + sp.y;
+  float force = -dot(normalize(sp), n) * length(sp);
+  if (force < 0.0f) force = 0.0f;
+  const float lift = (1.0f - collision) * length(sp);
+  const float capacity = force * hfac + 0.02f * lift * hfac;
+  const float diff = capacity - sed;
+  if (!(std::isfinite(diff) && std::isfinite(px) && std::isfinite(py) && std::isfinite(pz))) return false;
+  const float two32 = 4294967296.0f;
+  X.tq[0][ci] += to_fixed64(sed * two32);
+  X.tq[1][ci] += to_fixed64(sp.x * two32);
+  X.tq[2][ci] += to_fixed64(sp.y * two32);
+  X.tq[3][ci] += to_fixed64(sp.z * two32);
+  const int32_t ex_q = to_fixed(c.suspension * diff * scale);
+  X.D[ci] = wsub(X.D[ci], ex_q);
+  X.C[ci] += 1;
+  P.sed_q = wadd(P.sed_q, ex_q);
+  P.px = px; P.py = py; P.pz = pz;
+  P.vx = sp.x; P.vy = sp.y; P.vz = sp.z;
+  X.steps++;
+  return true;
+}
+
+// World::cascade in fixed point on a local height buffer (row stride ls):
+// in-bounds neighbours in the reference's order, stable descending by
+// height, each moving half the excess over the slope limit.
+int cascade_q(int32_t* L, int ls, int li, int lj, bool vx0, bool vx2, bool vz0, bool vz2, const so_params& c,
+              float scale, float inv) {
+  struct K { int k; int32_t key; };
+  const bool val[8] = {vx0 && vz0, vx0, vx0 && vz2, vz0, vz2, vx2 && vz0, vx2, vx2 && vz2};
+  K sn[8];
+  int num = 0;
+  for (int k = 0; k < 8; k++)
+    if (val[k]) sn[num++] = K{k, L[(li + NB_DX[k]) * ls + (lj + NB_DZ[k])]};
+  insertion_sort_desc(sn, num, [](const K& a, const K& b) { return a.key > b.key; });
+  int32_t& hc = L[li * ls + lj];
+  int t = 0;
+  for (int r = 0; r < num; r++) {
+    const int k = sn[r].k;
+    const float dx = (float)NB_DX[k], dz = (float)NB_DZ[k];
+    const float d = std::sqrt(dx * dx + dz * dz);
+    const int64_t dq = (int64_t)hc - (int64_t)sn[r].key;
+    if (dq == 0) continue;
+    const float excess = std::fabs((float)dq * inv) - d * c.maxdiff;
+    if (excess <= 0.0f) continue;
+    const int32_t tq = to_fixed(c.settling * excess / 2.0f * scale);
+    const int32_t sgn = dq > 0 ? tq : -tq;
+    int32_t& hn = L[(li + NB_DX[k]) * ls + (lj + NB_DZ[k])];
+    hc = wsub(hc, sgn);
+    hn = wadd(hn, sgn);
+    t++;
+  }
+  return t;
+}
+
+// One tile's share of a cascade pass.
+int64_t cascade_tile(so_world* w, int32_t* H, int32_t* D, int32_t* C, int tx, int tz) {
+  const int nx = w->nx, nz = w->nz;
+  const int x0 = tx * kTile, z0 = tz * kTile;
+  const int ls = kTile + 2;
+  int32_t L[(kTile + 2) * (kTile + 2)];
+  const float scale = (float)(1u << w->p.frac_bits);
+  const float inv = 1.0f / scale;
+  for (int i = 0; i < ls; i++)
+    for (int j = 0; j < ls; j++) {
+      const int x = x0 + i - 1, z = z0 + j - 1;
+      L[i * ls + j] = (x >= 0 && z >= 0 && x < nx && z < nz) ? wadd(H[(long)x * nz + z], D[(long)x * nz + z]) : 0;
+    }
+  int64_t transfers = 0;
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++)
+      for (int i = 0; i < kTile; i++)
+        for (int j = 0; j < kTile; j++) {
+          const int x = x0 + i, z = z0 + j;
+          if (x >= nx || z >= nz || x % 3 != a || z % 3 != b) continue;
+          const int cnt = C[(long)x * nz + z];
+          for (int r = 0; r < cnt; r++)
+            transfers += cascade_q(L, ls, i + 1, j + 1, x > 0, x + 1 < nx, z > 0, z + 1 < nz, w->p, scale, inv);
+        }
+  for (int i = 0; i < ls; i++)
+    for (int j = 0; j < ls; j++) {
+      const int x = x0 + i - 1, z = z0 + j - 1;
+      if (x < 0 || z < 0 || x >= nx || z >= nz) continue;
+      const long g = (long)x * nz + z;
+      const bool own = i >= 1 && j >= 1 && i <= kTile && j <= kTile;
+      if (own) {
+        H[g] = L[i * ls + j];
+        D[g] = 0;
+        C[g] = 0;
+      } else {
+        H[g] = wsub(L[i * ls + j], D[g]);
+      }
+    }
+  return transfers;
+}
+
+void ensure_fixed(so_world* w) {
+  if (w->hq_valid) return;
+  const size_t n = (size_t)w->nx * w->nz;
+  const float scale = (float)(1u << w->p.frac_bits);
+  w->hq.resize(n);
+  for (size_t i = 0; i < n; i++) w->hq[i] = to_fixed(w->f[0][i] * scale);
+  w->hq_valid = true;
+  w->exported_q = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_t* cycle_counter) {
+  ensure_fixed(w);
+  const size_t n = (size_t)w->nx * w->nz;
+  const float inv = 1.0f / (float)(1u << w->p.frac_bits);
+  const float lrate = w->p.lrate;
+  const int ntx = (w->nx + kTile - 1) / kTile, ntz = (w->nz + kTile - 1) / kTile;
+  std::vector<int64_t> tq[4];
+  for (auto& t : tq) t.assign(n, 0);
+  std::vector<int32_t> D(n, 0), C(n, 0);
+  std::vector<PState> live, next;
+  w->st_steps = w->st_particles = w->st_transfers = 0;
+  for (int cyc = 0; cyc < cycles; cyc++) {
+    const uint64_t cc = *cycle_counter;
+    ParCtx X;
+    X.w = w;
+    X.seed_lo = (uint32_t)seed; X.seed_hi = (uint32_t)(seed >> 32);
+    X.c_lo = (uint32_t)cc; X.c_hi = (uint32_t)(cc >> 32);
+    X.exported = X.steps = X.transfers = 0;
+    for (auto& t : tq) std::fill(t.begin(), t.end(), 0);
+    for (int k = 0; k < 4; k++) X.tq[k] = tq[k].data();
+    X.D = D.data();
+    X.C = C.data();
+    live.clear();
+    for (int i = 0; i < particles; i++) {
+      uint32_t u[4];
+      so_philox4x32((uint32_t)i, 0xFFFFFFFFu, X.c_lo, X.c_hi, X.seed_lo, X.seed_hi, u);
+      const int x = (int)(u[0] % (uint32_t)w->nx), z = (int)(u[1] % (uint32_t)w->nz);
+      const int fxq = (int)(u[2] % 1000u), fzq = (int)(u[3] % 1000u);
+      PState P;
+      P.id = i; P.age = 0; P.sed_q = 0;
+      P.px = (float)x + (float)fxq / 1000.0f; P.py = 0.0f; P.pz = (float)z + (float)fzq / 1000.0f;
+      P.vx = P.vy = P.vz = 0.0f;
+      live.push_back(P);
+    }
+    for (int step = 0; !live.empty(); step++) {
+      X.H = w->hq.data();
+      next.clear();
+      for (PState& P : live) {
+        if (par_fly(X, P, step)) next.push_back(P);
+        else X.exported += P.sed_q;
+      }
+      if (!next.empty())
+        for (int color = 0; color < 4; color++)
+          for (int tx = color >> 1; tx < ntx; tx += 2)
+            for (int tz = color & 1; tz < ntz; tz += 2)
+              X.transfers += cascade_tile(w, w->hq.data(), D.data(), C.data(), tx, tz);
+      live.swap(next);
+    }
+    for (size_t i = 0; i < n; i++) {
+      for (int k = 0; k < 4; k++) {
+        const float t = (float)tq[k][i] * 2.3283064365386963e-10f;
+        w->f[5 + k][i] = t;
+        w->f[1 + k][i] = (1.0f - lrate) * w->f[1 + k][i] + lrate * t;
+      }
+      w->f[0][i] = (float)w->hq[i] * inv;
+    }
+    w->exported_q += X.exported;
+    w->st_steps += X.steps;
+    w->st_particles += particles;
+    w->st_transfers += X.transfers;
+    *cycle_counter = cc + 1;
+  }
+}
+
+void so_par_get_heights_q(so_world* w, int32_t* dst) {
+  ensure_fixed(w);
+  std::memcpy(dst, w->hq.data(), sizeof(int32_t) * w->hq.size());
+}
+
+void so_par_ledger(so_world* w, int64_t* map_q, int64_t* exported_q) {
+  ensure_fixed(w);
+  int64_t s = 0;
+  for (int32_t v : w->hq) s += v;
+  *map_q = s;
+  *exported_q = w->exported_q;
+}
+
+}  // extern "C"
+
+extern "C" void so_expf_libm_bits(uint32_t first, long n, float* out) {
+  for (long i = 0; i < n; i++) {
+    const uint32_t u = first + (uint32_t)i;
+    float x;
+    std::memcpy(&x, &u, 4);
+    out[i] = std::exp(x);
+  }
+}

@@ -66,12 +66,14 @@ void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out);
 
 /* --- CPU model of the parallel fixed-point mode (bitwise model of the GPU
  *     kernels: same float operation order, same counter-based RNG). --- */
-
-
-
+void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_t* cycle_counter);
+void so_par_get_heights_q(so_world* w, int32_t* dst);
+void so_par_ledger(so_world* w, int64_t* map_q, int64_t* exported_q);
 void so_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
                    uint32_t* out4);
 float so_expf_poly(float x);
+/* The C library expf over n consecutive float bit patterns. */
+void so_expf_libm_bits(uint32_t first, long n, float* out);
 
 #ifdef __cplusplus
 }

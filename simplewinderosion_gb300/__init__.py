@@ -1,0 +1,299 @@
+"""GB300 SimpleWindErosion: the erosion hot path (World::erode, Wind::fly,
+World::cascade) as CUDA kernels for sm_103a behind a C ABI (include/swe.h).
+
+This module is the Python side of that ABI: a thin ctypes mirror of the
+reference's static simulation API (source/world.hpp:9-24, source/wind.hpp:4-26)
+used by the tests and the benchmark. All computation happens in
+libswe_gb300.so; there is no CPU fallback: without the built library the
+first World (or any library call) raises ImportError.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import _lib as _libmod
+from ._lib import lib_path
+
+__all__ = ["Params", "Field", "Mode", "World", "SweError", "lib", "lib_path", "FIELDS", "wind_direction"]
+
+
+class SweError(RuntimeError):
+    """A C-ABI call returned a negative status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"swe error {code}: {msg}")
+        self.code = code
+
+
+class Field(enum.IntEnum):
+    """Cell fields in quad::cell order (source/cellpool.h:226-240)."""
+
+    HEIGHT = 0
+    MASSFLOW = 1
+    MOMENTUMX = 2
+    MOMENTUMY = 3
+    MOMENTUMZ = 4
+    MASSFLOW_TRACK = 5
+    MOMENTUMX_TRACK = 6
+    MOMENTUMY_TRACK = 7
+    MOMENTUMZ_TRACK = 8
+
+
+FIELDS = list(Field)
+
+
+class Mode(enum.IntEnum):
+    ORDERED = 0   # particles in sequence, C library rand(): the reference's own order
+    PARALLEL = 1  # lock-step particles, fixed-point integer deposits
+
+
+class _CParams(ctypes.Structure):
+    _fields_ = [
+        ("max_age", ctypes.c_int),
+        ("boundarylayer", ctypes.c_float),
+        ("suspension", ctypes.c_float),
+        ("gravity", ctypes.c_float),
+        ("lrate", ctypes.c_float),
+        ("maxdiff", ctypes.c_float),
+        ("settling", ctypes.c_float),
+        ("mapscale", ctypes.c_float),
+        ("pspeed", ctypes.c_float * 3),
+        ("frac_bits", ctypes.c_int),
+    ]
+
+
+@dataclass
+class Params:
+    """Mirror of the reference statics; defaults are the reference's values:
+    Wind::maxAge/boundarylayer/suspension/gravity (wind.hpp:23-26),
+    World::lrate/maxdiff/settling (world.hpp:30-32), quad::mapscale
+    (cellpool.h:184), Wind::pspeed (wind.hpp:13). frac_bits is the parallel
+    mode's fixed-point resolution."""
+
+    max_age: int = 512
+    boundarylayer: float = 2.0
+    suspension: float = 0.05
+    gravity: float = 0.1
+    lrate: float = 0.1
+    maxdiff: float = 0.005
+    settling: float = 1.0
+    mapscale: float = 80.0
+    pspeed: tuple = (1.0, 0.0, 0.0)
+    frac_bits: int = 24
+
+    def to_c(self) -> _CParams:
+        c = _CParams()
+        for k in ("max_age", "boundarylayer", "suspension", "gravity", "lrate", "maxdiff", "settling",
+                  "mapscale", "frac_bits"):
+            setattr(c, k, getattr(self, k))
+        for i in range(3):
+            c.pspeed[i] = float(self.pspeed[i])
+        return c
+
+
+def wind_direction(x: float, y: float, z: float) -> tuple:
+    """glm::normalize of a wind vector in float32 arithmetic:
+    v * (1/sqrt(dot(v,v))), the prevailing wind the configs quote."""
+    v = np.array([x, y, z], dtype=np.float32)
+    d = np.float32(np.float32(v[0] * v[0] + v[1] * v[1]) + np.float32(v[2] * v[2]))
+    s = np.float32(np.float32(1.0) / np.sqrt(d, dtype=np.float32))
+    return tuple(float(np.float32(c * s)) for c in v)
+
+
+_P = ctypes.c_void_p
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+def _setup(L):
+    L.swe_params_default.argtypes = [ctypes.POINTER(_CParams)]
+    L.swe_world_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_CParams), ctypes.c_uint64,
+                                   ctypes.POINTER(_P)]
+    L.swe_world_destroy.argtypes = [_P]
+    L.swe_world_destroy.restype = None
+    L.swe_world_set_params.argtypes = [_P, ctypes.POINTER(_CParams)]
+    L.swe_world_upload.argtypes = [_P, ctypes.c_int, _P, ctypes.c_size_t]
+    L.swe_world_download.argtypes = [_P, ctypes.c_int, _P, ctypes.c_size_t]
+    L.swe_world_device_field.argtypes = [_P, ctypes.c_int, ctypes.POINTER(_P)]
+    L.swe_world_erode.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.swe_world_sync.argtypes = [_P]
+    L.swe_world_status.argtypes = [_P, ctypes.POINTER(ctypes.c_uint32)]
+    L.swe_world_seed_rand.argtypes = [_P, ctypes.c_uint32]
+    L.swe_world_set_rand_tape.argtypes = [_P, _P, ctypes.c_size_t]
+    L.swe_world_mass_ledger.argtypes = [_P, _i64p, _i64p, _i64p]
+    L.swe_world_stats.argtypes = [_P, _i64p, _i64p, _i64p]
+    L.swe_trace_particles.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, _P, _P]
+    L.swe_world_fly.argtypes = [_P, ctypes.c_float, ctypes.c_float, ctypes.c_int, _P, _P,
+                                ctypes.POINTER(ctypes.c_int)]
+    L.swe_world_cascade_at.argtypes = [_P, ctypes.c_int, ctypes.c_int]
+    L.swe_world_normals.argtypes = [_P, _P, ctypes.c_size_t]
+    L.swe_world_expf_bits.argtypes = [_P, ctypes.c_uint32, ctypes.c_size_t, _P]
+    L.swe_last_error.restype = ctypes.c_char_p
+    L.swe_last_error.argtypes = []
+
+
+class _Lazy:
+    """The library, loaded and typed on first attribute access."""
+
+    def __init__(self):
+        self._L = None
+
+    def __getattr__(self, name):
+        if self._L is None:
+            L = _libmod.load()
+            _setup(L)
+            self._L = L
+        return getattr(self._L, name)
+
+
+lib = _Lazy()
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise SweError(rc, lib.swe_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> _P:
+    return a.ctypes.data_as(_P)
+
+
+class World:
+    """One erosion world (the reference's `World` statics plus its map)."""
+
+    def __init__(self, nx: int, nz: int | None = None, params: Params | None = None, seed: int = 0):
+        self.nx = int(nx)
+        self.nz = int(nx if nz is None else nz)
+        self.params = params or Params()
+        self._h = _P()
+        cp = self.params.to_c()
+        _check(lib.swe_world_create(self.nx, self.nz, ctypes.byref(cp), ctypes.c_uint64(seed),
+                                    ctypes.byref(self._h)))
+
+    # -- lifetime
+    def close(self):
+        if self._h:
+            lib.swe_world_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def n(self) -> int:
+        return self.nx * self.nz
+
+    def set_params(self, params: Params):
+        cp = params.to_c()
+        _check(lib.swe_world_set_params(self._h, ctypes.byref(cp)))
+        self.params = params
+
+    # -- fields
+    def upload(self, f: Field, values) -> None:
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.float32).reshape(-1))
+        _check(lib.swe_world_upload(self._h, int(f), _ptr(a), a.size))
+
+    def download(self, f: Field) -> np.ndarray:
+        a = np.empty(self.n, dtype=np.float32)
+        _check(lib.swe_world_download(self._h, int(f), _ptr(a), a.size))
+        return a.reshape(self.nx, self.nz)
+
+    def device_field(self, f: Field) -> int:
+        p = _P()
+        _check(lib.swe_world_device_field(self._h, int(f), ctypes.byref(p)))
+        return int(p.value or 0)
+
+    @property
+    def height(self) -> np.ndarray:
+        return self.download(Field.HEIGHT)
+
+    @height.setter
+    def height(self, v):
+        self.upload(Field.HEIGHT, v)
+
+    # -- simulation (World::erode, world.hpp:36-77)
+    def erode(self, particles: int, cycles: int = 1, mode: Mode = Mode.PARALLEL, sync: bool = True) -> None:
+        _check(lib.swe_world_erode(self._h, int(cycles), int(particles), int(mode)))
+        if sync:
+            self.sync()
+
+    def sync(self) -> None:
+        _check(lib.swe_world_sync(self._h))
+
+    def status(self) -> int:
+        s = ctypes.c_uint32()
+        _check(lib.swe_world_status(self._h, ctypes.byref(s)))
+        return int(s.value)
+
+    def seed_rand(self, seed: int) -> None:
+        _check(lib.swe_world_seed_rand(self._h, ctypes.c_uint32(seed)))
+
+    def set_rand_tape(self, tape) -> None:
+        if tape is None:
+            _check(lib.swe_world_set_rand_tape(self._h, None, 0))
+            return
+        a = np.ascontiguousarray(np.asarray(tape, dtype=np.int32).reshape(-1))
+        _check(lib.swe_world_set_rand_tape(self._h, _ptr(a), a.size))
+
+    def mass_ledger(self) -> tuple[int, int, int]:
+        m, i, e = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib.swe_world_mass_ledger(self._h, ctypes.byref(m), ctypes.byref(i), ctypes.byref(e)))
+        return m.value, i.value, e.value
+
+    def stats(self) -> tuple[int, int, int]:
+        s, p, t = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib.swe_world_stats(self._h, ctypes.byref(s), ctypes.byref(p), ctypes.byref(t)))
+        return s.value, p.value, t.value
+
+    # -- unit-level entry points
+    def trace(self, spawn_xz, steps: int, tape) -> np.ndarray:
+        """Frozen-map trajectories; returns (n, steps, 9) records
+        (alive, age, pos.xyz, speed.xyz, sediment)."""
+        s = np.ascontiguousarray(np.asarray(spawn_xz, dtype=np.float32).reshape(-1, 2))
+        n = s.shape[0]
+        t = np.ascontiguousarray(np.asarray(tape, dtype=np.int32).reshape(-1))
+        if t.size != n * steps * 3:
+            raise ValueError("tape must hold 3 values per particle step")
+        out = np.empty((n, steps, 9), dtype=np.float32)
+        _check(lib.swe_trace_particles(self._h, _ptr(s), n, int(steps), _ptr(t), _ptr(out)))
+        return out
+
+    def fly(self, x: float, z: float, steps: int, tape=None) -> tuple[np.ndarray, int]:
+        out = np.empty((steps, 9), dtype=np.float32)
+        ok = ctypes.c_int()
+        tp = None
+        if tape is not None:
+            tp = np.ascontiguousarray(np.asarray(tape, dtype=np.int32).reshape(-1))
+            if tp.size != steps * 3:
+                raise ValueError("tape must hold 3 values per step")
+        _check(lib.swe_world_fly(self._h, ctypes.c_float(x), ctypes.c_float(z), int(steps),
+                                 _ptr(tp) if tp is not None else None, _ptr(out), ctypes.byref(ok)))
+        return out, ok.value
+
+    def cascade(self, x: int, z: int) -> None:
+        _check(lib.swe_world_cascade_at(self._h, int(x), int(z)))
+
+    def expf_bits(self, first_bits: int, n: int) -> np.ndarray:
+        """The device's reference-compatible expf over n consecutive float bit
+        patterns starting at first_bits."""
+        out = np.empty(n, dtype=np.float32)
+        _check(lib.swe_world_expf_bits(self._h, ctypes.c_uint32(first_bits), n, _ptr(out)))
+        return out
+
+    def normals(self) -> np.ndarray:
+        out = np.empty(self.n * 3, dtype=np.float32)
+        _check(lib.swe_world_normals(self._h, _ptr(out), out.size))
+        return out.reshape(self.nx, self.nz, 3)

@@ -1,0 +1,595 @@
+// C ABI of the library (include/swe.h): the world object that owns the
+// device-resident cell maps and drives the kernels on its own stream.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swe.h"
+#include "swe_kernels.h"
+
+using swe::Consts;
+using swe::Counters;
+using swe::Fields;
+using swe::GlibcRandState;
+
+// The build-time list of arguments where the C library expf is not the
+// correctly rounded value (swe_libm_table.cpp, gen_libm_expf.cpp):
+// uint32 count, count sorted uint32 bit patterns, count int8 directions.
+extern "C" const unsigned char swe_libm_expf_blob[];
+extern "C" const unsigned char swe_libm_expf_blob_end[];
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+#define SWE_CK(call)                                                                    \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      return fail(e_ == cudaErrorMemoryAllocation ? SWE_ERR_NO_MEMORY : SWE_ERR_CUDA,   \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    }                                                                                   \
+  } while (0)
+
+// Host side of the C library rand() replica (same recurrence as the device
+// side in swe_exact.cu): seeds r[0] = seed, r[i] = 16807 r[i-1] mod (2^31-1)
+// for i < 31, r[i] = r[i-31] for i = 31..33, then discards 310 elements of
+// r[i] = r[i-31] + r[i-3].
+uint32_t glibc_step(GlibcRandState& g) {
+  int h = g.head;
+  int a = h + 3;  if (a >= 34) a -= 34;
+  int b = h + 31; if (b >= 34) b -= 34;
+  const uint32_t v = g.r[a] + g.r[b];
+  g.r[h] = v;
+  g.head = (h + 1 == 34) ? 0 : h + 1;
+  return v;
+}
+
+void glibc_seed(GlibcRandState& g, uint32_t seed) {
+  const int32_t s = (int32_t)(seed == 0 ? 1u : seed);
+  int32_t t[31];
+  t[0] = s;
+  for (int i = 1; i < 31; i++) {
+    long long v = (16807LL * (long long)t[i - 1]) % 2147483647LL;
+    if (v < 0) v += 2147483647LL;
+    t[i] = (int32_t)v;
+  }
+  for (int i = 0; i < 31; i++) g.r[i] = (uint32_t)t[i];
+  for (int i = 31; i < 34; i++) g.r[i] = g.r[i - 31];
+  g.head = 0;  // element 34 goes to slot 0
+  g.pad = 0;
+  for (int i = 0; i < 310; i++) glibc_step(g);
+}
+
+bool params_ok(const swe_params& p, std::string& why) {
+  if (p.max_age < 0 || p.max_age > 1000000) { why = "max_age must be in [0, 1e6]"; return false; }
+  if (p.frac_bits < 8 || p.frac_bits > 28) { why = "frac_bits must be in [8, 28]"; return false; }
+  if (!(p.boundarylayer != 0.0f)) { why = "boundarylayer must be non-zero"; return false; }
+  return true;
+}
+
+}  // namespace
+
+struct swe_world {
+  int nx = 0, nz = 0;
+  long n = 0;
+  swe_params p{};
+  uint64_t seed = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Fields F{};
+  float* fbase = nullptr;
+  Counters* cnt = nullptr;
+  GlibcRandState* grand = nullptr;
+  int32_t* tape = nullptr;
+  long long tape_len = 0;
+  // parallel mode
+  int32_t* hq = nullptr;      // 3n: heights, exchange deltas, visit counts
+  long long* tq = nullptr;    // 4n
+  void* pstate = nullptr;     // 2 buffers x 9 arrays x capacity
+  int pcap = 0;
+  swe::ParallelBuffers pb{};
+  bool hq_valid = false;
+  int step_grid = 0;
+  long long* dsum = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int g_particles = -1;
+  uint32_t* expf_x = nullptr;  // device copy of the expf exception list
+  int8_t* expf_d = nullptr;
+  int expf_n = 0;
+
+  Consts consts() const {
+    Consts c;
+    c.nx = nx; c.nz = nz;
+    c.max_age = p.max_age;
+    c.boundarylayer = p.boundarylayer; c.suspension = p.suspension; c.gravity = p.gravity;
+    c.lrate = p.lrate; c.maxdiff = p.maxdiff; c.settling = p.settling; c.mapscale = p.mapscale;
+    c.px = p.pspeed[0]; c.py = p.pspeed[1]; c.pz = p.pspeed[2];
+    c.frac_bits = p.frac_bits;
+    c.scale = (float)(1u << p.frac_bits);
+    c.inv_scale = 1.0f / c.scale;
+    c.expf_x = expf_x;
+    c.expf_d = expf_d;
+    c.expf_n = expf_n;
+    return c;
+  }
+
+  void drop_graph() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    g_particles = -1;
+  }
+};
+
+namespace {
+
+int use_device(swe_world* w) {
+  SWE_CK(cudaSetDevice(w->device));
+  return SWE_OK;
+}
+
+// Parallel-mode buffers, grown to hold `particles`.
+int ensure_parallel(swe_world* w, int particles) {
+  if (!w->hq) {
+    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 3 * w->n));
+    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 3 * w->n, w->stream));
+    SWE_CK(cudaMalloc(&w->tq, sizeof(long long) * 4 * w->n));
+    SWE_CK(cudaMemsetAsync(w->tq, 0, sizeof(long long) * 4 * w->n, w->stream));
+    SWE_CK(cudaMalloc(&w->dsum, sizeof(long long)));
+    w->step_grid = swe::par_step_grid(w->device);
+  }
+  if (particles > w->pcap || !w->pstate) {
+    const int cap = particles > 0 ? particles : 1;
+    if (w->pstate) SWE_CK(cudaFree(w->pstate));
+    w->pstate = nullptr;
+    SWE_CK(cudaMalloc(&w->pstate, sizeof(int32_t) * 9 * 2 * (size_t)cap));
+    w->pcap = cap;
+    w->drop_graph();
+  }
+  swe::ParallelBuffers& B = w->pb;
+  B.hq = w->hq;
+  B.dq = w->hq + w->n;
+  B.visits = w->hq + 2 * w->n;
+  for (int k = 0; k < 4; k++) B.tq[k] = w->tq + (size_t)k * w->n;
+  int32_t* base = reinterpret_cast<int32_t*>(w->pstate);
+  for (int b = 0; b < 2; b++) {
+    int32_t* s = base + (size_t)b * 9 * w->pcap;
+    swe::ParticleSoA& S = B.state[b];
+    S.id = s;
+    S.age = s + 1 * (size_t)w->pcap;
+    S.px = reinterpret_cast<float*>(s + 2 * (size_t)w->pcap);
+    S.py = reinterpret_cast<float*>(s + 3 * (size_t)w->pcap);
+    S.pz = reinterpret_cast<float*>(s + 4 * (size_t)w->pcap);
+    S.vx = reinterpret_cast<float*>(s + 5 * (size_t)w->pcap);
+    S.vy = reinterpret_cast<float*>(s + 6 * (size_t)w->pcap);
+    S.vz = reinterpret_cast<float*>(s + 7 * (size_t)w->pcap);
+    S.sed_q = s + 8 * (size_t)w->pcap;
+  }
+  B.capacity = w->pcap;
+  return SWE_OK;
+}
+
+int ensure_fixed(swe_world* w) {
+  if (w->hq_valid) return SWE_OK;
+  const Consts c = w->consts();
+  swe::launch_height_to_fixed(w->F.f[0], w->pb.hq, c, w->cnt, w->stream);
+  SWE_CK(cudaGetLastError());
+  w->hq_valid = true;
+  return SWE_OK;
+}
+
+// Enqueue one parallel erode cycle (spawn, max_age+2 fly + cascade steps, EMA).
+int enqueue_parallel_cycle(swe_world* w, int particles) {
+  const Consts c = w->consts();
+  swe::launch_par_spawn(w->pb, c, w->seed, w->cnt, particles, w->n, w->stream);
+  const int nsteps = w->p.max_age + 2;
+  for (int t = 0; t < nsteps; t++) {
+    swe::launch_par_fly(w->pb, c, w->seed, w->cnt, t, w->step_grid, w->stream);
+    swe::launch_par_cascade(w->pb, c, w->cnt, t, w->stream);
+  }
+  swe::launch_par_ema(w->pb, w->F, c, w->cnt, w->n, w->stream);
+  SWE_CK(cudaGetLastError());
+  return SWE_OK;
+}
+
+int build_graph(swe_world* w, int particles) {
+  w->drop_graph();
+  cudaGraph_t g = nullptr;
+  SWE_CK(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_parallel_cycle(w, particles);
+  cudaError_t e = cudaStreamEndCapture(w->stream, &g);
+  if (rc != SWE_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  SWE_CK(e);
+  e = cudaGraphInstantiate(&w->gexec, g, 0);
+  cudaGraphDestroy(g);
+  SWE_CK(e);
+  w->g_particles = particles;
+  return SWE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void swe_params_default(swe_params* p) {
+  if (!p) return;
+  p->max_age = 512;
+  p->boundarylayer = 2.0f;
+  p->suspension = 0.05f;
+  p->gravity = 0.1f;
+  p->lrate = 0.1f;
+  p->maxdiff = 0.005f;
+  p->settling = 1.0f;
+  p->mapscale = 80.0f;
+  p->pspeed[0] = 1.0f;
+  p->pspeed[1] = 0.0f;
+  p->pspeed[2] = 0.0f;
+  p->frac_bits = 24;
+}
+
+const char* swe_last_error(void) { return g_error.c_str(); }
+
+int swe_world_create(int nx, int nz, const swe_params* p, uint64_t seed, swe_world** out) {
+  if (!out) return fail(SWE_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (nx < 1 || nz < 1) return fail(SWE_ERR_INVALID, "nx and nz must be >= 1");
+  if ((long long)nx * nz >= (1LL << 31)) return fail(SWE_ERR_INVALID, "nx*nz must be < 2^31");
+  swe_params prm;
+  if (p) prm = *p; else swe_params_default(&prm);
+  std::string why;
+  if (!params_ok(prm, why)) return fail(SWE_ERR_INVALID, why);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(SWE_ERR_CUDA, "no CUDA device available");
+  }
+  swe_world* w = new swe_world();
+  w->nx = nx; w->nz = nz; w->n = (long)nx * nz;
+  w->p = prm;
+  w->seed = seed;
+  int rc = SWE_OK;
+  auto init = [&]() -> int {
+    SWE_CK(cudaGetDevice(&w->device));
+    SWE_CK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    SWE_CK(cudaMalloc(&w->fbase, sizeof(float) * 9 * (size_t)w->n));
+    for (int k = 0; k < 9; k++) w->F.f[k] = w->fbase + (size_t)k * w->n;
+    SWE_CK(cudaMemsetAsync(w->fbase, 0, sizeof(float) * 9 * (size_t)w->n, w->stream));
+    SWE_CK(cudaMalloc(&w->cnt, sizeof(Counters)));
+    SWE_CK(cudaMemsetAsync(w->cnt, 0, sizeof(Counters), w->stream));
+    {
+      uint32_t cnt = 0;
+      std::memcpy(&cnt, swe_libm_expf_blob, 4);
+      const size_t blob = (size_t)(swe_libm_expf_blob_end - swe_libm_expf_blob);
+      if (blob != 4 + 5 * (size_t)cnt) return fail(SWE_ERR_INVALID, "embedded expf table is malformed");
+      w->expf_n = (int)cnt;
+      SWE_CK(cudaMalloc(&w->expf_x, 4 * (size_t)cnt + 4));
+      SWE_CK(cudaMalloc(&w->expf_d, (size_t)cnt + 4));
+      SWE_CK(cudaMemcpyAsync(w->expf_x, swe_libm_expf_blob + 4, 4 * (size_t)cnt, cudaMemcpyHostToDevice, w->stream));
+      SWE_CK(cudaMemcpyAsync(w->expf_d, swe_libm_expf_blob + 4 + 4 * (size_t)cnt, cnt, cudaMemcpyHostToDevice,
+                             w->stream));
+    }
+    SWE_CK(cudaMalloc(&w->grand, sizeof(GlibcRandState)));
+    GlibcRandState g;
+    glibc_seed(g, (uint32_t)seed);
+    SWE_CK(cudaMemcpyAsync(w->grand, &g, sizeof(g), cudaMemcpyHostToDevice, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    return SWE_OK;
+  };
+  rc = init();
+  if (rc != SWE_OK) {
+    std::string msg = g_error;
+    swe_world_destroy(w);
+    g_error = msg;
+    return rc;
+  }
+  *out = w;
+  return SWE_OK;
+}
+
+void swe_world_destroy(swe_world* w) {
+  if (!w) return;
+  cudaSetDevice(w->device);
+  if (w->stream) cudaStreamSynchronize(w->stream);
+  w->drop_graph();
+  cudaFree(w->fbase);
+  cudaFree(w->cnt);
+  cudaFree(w->grand);
+  cudaFree(w->tape);
+  cudaFree(w->hq);
+  cudaFree(w->tq);
+  cudaFree(w->pstate);
+  cudaFree(w->dsum);
+  cudaFree(w->expf_x);
+  cudaFree(w->expf_d);
+  if (w->stream) cudaStreamDestroy(w->stream);
+  delete w;
+}
+
+int swe_world_set_params(swe_world* w, const swe_params* p) {
+  if (!w || !p) return fail(SWE_ERR_INVALID, "NULL argument");
+  std::string why;
+  if (!params_ok(*p, why)) return fail(SWE_ERR_INVALID, why);
+  if (p->frac_bits != w->p.frac_bits) w->hq_valid = false;
+  w->p = *p;
+  w->drop_graph();
+  return SWE_OK;
+}
+
+int swe_world_get_params(swe_world* w, swe_params* p) {
+  if (!w || !p) return fail(SWE_ERR_INVALID, "NULL argument");
+  *p = w->p;
+  return SWE_OK;
+}
+
+int swe_world_size(swe_world* w, int* nx, int* nz) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (nx) *nx = w->nx;
+  if (nz) *nz = w->nz;
+  return SWE_OK;
+}
+
+int swe_world_upload(swe_world* w, swe_field f, const float* host, size_t n) {
+  if (!w || !host) return fail(SWE_ERR_INVALID, "NULL argument");
+  if ((int)f < 0 || (int)f > 8) return fail(SWE_ERR_INVALID, "unknown field");
+  if (n != (size_t)w->n) return fail(SWE_ERR_INVALID, "n must equal nx*nz");
+  if (int rc = use_device(w)) return rc;
+  SWE_CK(cudaMemcpyAsync(w->F.f[f], host, sizeof(float) * n, cudaMemcpyHostToDevice, w->stream));
+  if (f == SWE_HEIGHT) {
+    w->hq_valid = false;
+    SWE_CK(cudaMemsetAsync(&w->cnt->exported_q, 0, sizeof(long long), w->stream));
+  }
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  return SWE_OK;
+}
+
+int swe_world_download(swe_world* w, swe_field f, float* host, size_t n) {
+  if (!w || !host) return fail(SWE_ERR_INVALID, "NULL argument");
+  if ((int)f < 0 || (int)f > 8) return fail(SWE_ERR_INVALID, "unknown field");
+  if (n != (size_t)w->n) return fail(SWE_ERR_INVALID, "n must equal nx*nz");
+  if (int rc = use_device(w)) return rc;
+  SWE_CK(cudaMemcpyAsync(host, w->F.f[f], sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  return SWE_OK;
+}
+
+int swe_world_device_field(swe_world* w, swe_field f, void** dev_ptr) {
+  if (!w || !dev_ptr) return fail(SWE_ERR_INVALID, "NULL argument");
+  if ((int)f < 0 || (int)f > 8) return fail(SWE_ERR_INVALID, "unknown field");
+  *dev_ptr = w->F.f[f];
+  return SWE_OK;
+}
+
+int swe_world_erode(swe_world* w, int cycles, int particles, swe_mode mode) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (cycles < 0 || particles < 0) return fail(SWE_ERR_INVALID, "cycles and particles must be >= 0");
+  if (mode != SWE_MODE_ORDERED && mode != SWE_MODE_PARALLEL) return fail(SWE_ERR_INVALID, "unknown mode");
+  if (int rc = use_device(w)) return rc;
+  SWE_CK(cudaMemsetAsync(w->cnt, 0, 3 * sizeof(unsigned long long), w->stream));
+  if (cycles == 0) return SWE_OK;
+  const Consts c = w->consts();
+  if (mode == SWE_MODE_ORDERED) {
+    for (int k = 0; k < cycles; k++) {
+      swe::launch_reset_tracks(w->F, w->n, w->stream);
+      swe::launch_ordered_particles(w->F, c, w->grand, w->tape, w->tape_len, w->cnt, particles, w->stream);
+      swe::launch_ema_float(w->F, c.lrate, w->n, w->stream);
+    }
+    SWE_CK(cudaGetLastError());
+    w->hq_valid = false;
+    return SWE_OK;
+  }
+  if (int rc = ensure_parallel(w, particles)) return rc;
+  if (int rc = ensure_fixed(w)) return rc;
+  if (!w->gexec || w->g_particles != particles) {
+    if (int rc = build_graph(w, particles)) return rc;
+  }
+  for (int k = 0; k < cycles; k++) SWE_CK(cudaGraphLaunch(w->gexec, w->stream));
+  return SWE_OK;
+}
+
+int swe_world_status(swe_world* w, uint32_t* status) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  unsigned int st = 0;
+  SWE_CK(cudaMemcpy(&st, &w->cnt->status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (status) *status = st;
+  return SWE_OK;
+}
+
+int swe_world_sync(swe_world* w) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  uint32_t st = 0;
+  if (int rc = swe_world_status(w, &st)) return rc;
+  if (st) {
+    SWE_CK(cudaMemset(&w->cnt->status, 0, sizeof(unsigned int)));
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "device status 0x%x:%s%s%s", st, (st & SWE_STATUS_NONFINITE) ? " non-finite particle" : "",
+                  (st & SWE_STATUS_RANGE) ? " fixed-point height out of range" : "",
+                  (st & SWE_STATUS_TAPE) ? " rand tape exhausted" : "");
+    return fail(SWE_ERR_DEVICE, buf);
+  }
+  return SWE_OK;
+}
+
+int swe_world_seed_rand(swe_world* w, uint32_t seed) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  GlibcRandState g;
+  glibc_seed(g, seed);
+  SWE_CK(cudaMemcpyAsync(w->grand, &g, sizeof(g), cudaMemcpyHostToDevice, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  return SWE_OK;
+}
+
+int swe_world_set_rand_tape(swe_world* w, const int32_t* tape, size_t n) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (n > 0 && !tape) return fail(SWE_ERR_INVALID, "tape is NULL");
+  if (int rc = use_device(w)) return rc;
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  if (w->tape) SWE_CK(cudaFree(w->tape));
+  w->tape = nullptr;
+  w->tape_len = 0;
+  if (n > 0) {
+    SWE_CK(cudaMalloc(&w->tape, sizeof(int32_t) * n));
+    SWE_CK(cudaMemcpy(w->tape, tape, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    w->tape_len = (long long)n;
+  }
+  SWE_CK(cudaMemset(&w->cnt->tape_pos, 0, sizeof(long long)));
+  return SWE_OK;
+}
+
+int swe_world_mass_ledger(swe_world* w, int64_t* map_q, int64_t* inflight_q, int64_t* exported_q) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  if (int rc = ensure_parallel(w, 0)) return rc;
+  if (int rc = ensure_fixed(w)) return rc;
+  SWE_CK(cudaMemsetAsync(w->dsum, 0, sizeof(long long), w->stream));
+  swe::launch_sum_fixed(w->pb.hq, w->n, w->dsum, w->stream);
+  SWE_CK(cudaGetLastError());
+  long long s = 0, e = 0;
+  SWE_CK(cudaMemcpyAsync(&s, w->dsum, sizeof(s), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaMemcpyAsync(&e, &w->cnt->exported_q, sizeof(e), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  if (map_q) *map_q = s;
+  if (inflight_q) *inflight_q = 0;
+  if (exported_q) *exported_q = e;
+  return SWE_OK;
+}
+
+int swe_world_stats(swe_world* w, int64_t* particle_steps, int64_t* particles, int64_t* transfers) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  unsigned long long v[3] = {0, 0, 0};
+  SWE_CK(cudaMemcpyAsync(v, w->cnt, sizeof(v), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  if (particle_steps) *particle_steps = (int64_t)v[0];
+  if (particles) *particles = (int64_t)v[1];
+  if (transfers) *transfers = (int64_t)v[2];
+  return SWE_OK;
+}
+
+int swe_trace_particles(swe_world* w, const float* spawn_xz, int n, int steps, const int32_t* turb_tape,
+                        float* out_state) {
+  if (!w || !spawn_xz || !turb_tape || !out_state) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (n < 0 || steps < 0) return fail(SWE_ERR_INVALID, "n and steps must be >= 0");
+  if (n == 0 || steps == 0) return SWE_OK;
+  if (int rc = use_device(w)) return rc;
+  const size_t nrec = (size_t)n * steps;
+  float* d_spawn = nullptr;
+  int32_t* d_tape = nullptr;
+  float* d_out = nullptr;
+  int rc = SWE_OK;
+  auto run = [&]() -> int {
+    SWE_CK(cudaMalloc(&d_spawn, sizeof(float) * 2 * n));
+    SWE_CK(cudaMalloc(&d_tape, sizeof(int32_t) * 3 * nrec));
+    SWE_CK(cudaMalloc(&d_out, sizeof(float) * 9 * nrec));
+    SWE_CK(cudaMemcpyAsync(d_spawn, spawn_xz, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, w->stream));
+    SWE_CK(cudaMemcpyAsync(d_tape, turb_tape, sizeof(int32_t) * 3 * nrec, cudaMemcpyHostToDevice, w->stream));
+    swe::launch_trace(w->F.f[0], w->consts(), d_spawn, n, steps, d_tape, d_out, w->stream);
+    SWE_CK(cudaGetLastError());
+    SWE_CK(cudaMemcpyAsync(out_state, d_out, sizeof(float) * 9 * nrec, cudaMemcpyDeviceToHost, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    return SWE_OK;
+  };
+  rc = run();
+  cudaFree(d_spawn);
+  cudaFree(d_tape);
+  cudaFree(d_out);
+  return rc;
+}
+
+int swe_world_fly(swe_world* w, float x, float z, int steps, const int32_t* turb_tape, float* out_state,
+                  int* ok_steps) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (steps < 0) return fail(SWE_ERR_INVALID, "steps must be >= 0");
+  if (int rc = use_device(w)) return rc;
+  int32_t* d_tape = nullptr;
+  float* d_out = nullptr;
+  int* d_ok = nullptr;
+  auto run = [&]() -> int {
+    if (turb_tape && steps > 0) {
+      SWE_CK(cudaMalloc(&d_tape, sizeof(int32_t) * 3 * (size_t)steps));
+      SWE_CK(cudaMemcpyAsync(d_tape, turb_tape, sizeof(int32_t) * 3 * (size_t)steps, cudaMemcpyHostToDevice,
+                             w->stream));
+    }
+    if (out_state && steps > 0) SWE_CK(cudaMalloc(&d_out, sizeof(float) * 9 * (size_t)steps));
+    SWE_CK(cudaMalloc(&d_ok, sizeof(int)));
+    swe::launch_fly_live(w->F, w->consts(), x, z, steps, d_tape, w->grand, d_out, d_ok, w->cnt, w->stream);
+    SWE_CK(cudaGetLastError());
+    if (d_out)
+      SWE_CK(cudaMemcpyAsync(out_state, d_out, sizeof(float) * 9 * (size_t)steps, cudaMemcpyDeviceToHost,
+                             w->stream));
+    int ok = 0;
+    SWE_CK(cudaMemcpyAsync(&ok, d_ok, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    if (ok_steps) *ok_steps = ok;
+    return SWE_OK;
+  };
+  int rc = run();
+  cudaFree(d_tape);
+  cudaFree(d_out);
+  cudaFree(d_ok);
+  w->hq_valid = false;
+  return rc;
+}
+
+int swe_world_cascade_at(swe_world* w, int x, int z) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (x < 0 || z < 0 || x >= w->nx || z >= w->nz) return fail(SWE_ERR_INVALID, "cell out of bounds");
+  if (int rc = use_device(w)) return rc;
+  swe::launch_cascade_at(w->F.f[0], w->consts(), x, z, w->stream);
+  SWE_CK(cudaGetLastError());
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  w->hq_valid = false;
+  return SWE_OK;
+}
+
+int swe_world_normals(swe_world* w, float* host_out, size_t n) {
+  if (!w || !host_out) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (n != 3 * (size_t)w->n) return fail(SWE_ERR_INVALID, "n must equal 3*nx*nz");
+  if (int rc = use_device(w)) return rc;
+  float* d_out = nullptr;
+  auto run = [&]() -> int {
+    SWE_CK(cudaMalloc(&d_out, sizeof(float) * n));
+    swe::launch_normals(w->F.f[0], w->consts(), d_out, w->stream);
+    SWE_CK(cudaGetLastError());
+    SWE_CK(cudaMemcpyAsync(host_out, d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    return SWE_OK;
+  };
+  int rc = run();
+  cudaFree(d_out);
+  return rc;
+}
+
+int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host_y) {
+  if (!w || !host_y) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (n == 0) return SWE_OK;
+  if ((uint64_t)first_bits + n > (1ull << 32)) return fail(SWE_ERR_INVALID, "bit range exceeds 32 bits");
+  if (int rc = use_device(w)) return rc;
+  float* d_out = nullptr;
+  auto run = [&]() -> int {
+    SWE_CK(cudaMalloc(&d_out, sizeof(float) * n));
+    swe::launch_expf_bits(w->consts(), first_bits, (long)n, d_out, w->stream);
+    SWE_CK(cudaGetLastError());
+    SWE_CK(cudaMemcpyAsync(host_y, d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    return SWE_OK;
+  };
+  int rc = run();
+  cudaFree(d_out);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+// Host-side launchers of the erosion kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "swe_types.h"
+
+namespace swe {
+
+// Nine float fields in quad::cell order (cellpool.h:226-240).
+struct Fields {
+  float* f[9];
+};
+
+// ---- exact modes (swe_exact.cu) ----
+void launch_reset_tracks(const Fields& F, long n, cudaStream_t s);
+void launch_ema_float(const Fields& F, float lrate, long n, cudaStream_t s);
+void launch_ordered_particles(const Fields& F, const Consts& c, GlibcRandState* rng, const int32_t* tape,
+                              long long tape_len, Counters* cnt, int particles, cudaStream_t s);
+void launch_trace(const float* height, const Consts& c, const float* spawn_xz, int n, int steps,
+                  const int32_t* tape, float* out, cudaStream_t s);
+void launch_fly_live(const Fields& F, const Consts& c, float x, float z, int steps, const int32_t* tape,
+                     GlibcRandState* rng, float* out, int* ok_steps, Counters* cnt, cudaStream_t s);
+void launch_cascade_at(float* height, const Consts& c, int x, int z, cudaStream_t s);
+void launch_normals(const float* height, const Consts& c, float* out, cudaStream_t s);
+void launch_expf_bits(const Consts& c, uint32_t first, long n, float* out, cudaStream_t s);
+
+// ---- parallel fixed-point mode (swe_parallel.cu) ----
+struct ParallelBuffers {
+  int32_t* hq;         // fixed-point heights
+  int32_t* dq;         // exchange deltas pending for the cascade passes (zero between steps)
+  int32_t* visits;     // cascades owed per cell (zero between steps)
+  long long* tq[4];    // track accumulators (massflow, momx, momy, momz), 2^-32 units
+  ParticleSoA state[2];
+  int capacity;        // particles the state buffers hold
+};
+
+void launch_height_to_fixed(const float* height, int32_t* q, const Consts& c, Counters* cnt, cudaStream_t s);
+void launch_par_spawn(const ParallelBuffers& B, const Consts& c, uint64_t seed, Counters* cnt, int particles,
+                      long n_cells, cudaStream_t s);
+void launch_par_fly(const ParallelBuffers& B, const Consts& c, uint64_t seed, Counters* cnt, int step, int grid,
+                    cudaStream_t s);
+void launch_par_cascade(const ParallelBuffers& B, const Consts& c, Counters* cnt, int step, cudaStream_t s);
+void launch_par_ema(const ParallelBuffers& B, const Fields& F, const Consts& c, Counters* cnt, long n_cells,
+                    cudaStream_t s);
+int par_step_grid(int device);
+void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s);
+
+}  // namespace swe

@@ -1,0 +1,59 @@
+// Plain structs shared by the host world object and the kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace swe {
+
+// Constants of one world, passed to kernels by value (mirrors swe_params).
+struct Consts {
+  int nx, nz;
+  int max_age;
+  float boundarylayer, suspension, gravity, lrate, maxdiff, settling, mapscale;
+  float px, py, pz;  // prevailing wind (Wind::pspeed)
+  int frac_bits;
+  float scale;      // 2^frac_bits
+  float inv_scale;  // 2^-frac_bits
+  // Arguments where the C library expf is not the correctly rounded value
+  // (sorted bit patterns) and the direction of its one-ulp difference.
+  const uint32_t* expf_x;
+  const int8_t* expf_d;
+  int expf_n;
+};
+
+// State of the C library rand() replica: the last 34 elements of the
+// additive feedback recurrence r[i] = r[i-31] + r[i-3] (mod 2^32), element i
+// in slot i % 34, and the slot of the next element to produce.
+struct GlibcRandState {
+  uint32_t r[34];
+  int head;
+  int pad;
+};
+
+// Device-side counters of one world (one allocation, zeroed per erode call).
+struct Counters {
+  unsigned long long particle_steps;
+  unsigned long long particles;
+  unsigned long long transfers;
+  long long exported_q;      // cumulative since the last height upload
+  int live[2];               // parallel mode: live particles per step parity
+  unsigned int status;       // SWE_STATUS_* bits
+  unsigned int pad;
+  long long tape_pos;        // ordered mode tape cursor
+  unsigned long long cycle;  // parallel mode: cycles completed (RNG counter)
+};
+
+// Particle state of the parallel mode, structure of arrays.
+struct ParticleSoA {
+  int* id;
+  int* age;
+  float* px;
+  float* py;
+  float* pz;
+  float* vx;
+  float* vy;
+  float* vz;
+  int* sed_q;
+};
+
+}  // namespace swe

@@ -1,0 +1,218 @@
+"""CUDA exact-semantics kernels against the CPU oracle and the reference's
+golden outputs, through the C ABI.
+
+The oracle port runs on this machine with its C library (rand, expf), i.e.
+computes what the reference binary computes here; the kernels reproduce the
+C library's expf through a build-time exception list, so the bars are:
+- normals, cascade, fly, ordered erode, frozen-map traces: bit-identical to
+  the oracle port;
+- frozen-map trajectories (check a): |gpu - ref| <= 1e-5 * max(1, |ref|) for
+  positions, speeds and sediment (met with equality);
+- ordered erode after 100 cycles at 256^2 x 1000 particles (check b): heights
+  within 1e-4 absolute (met with equality);
+- against the golden fixtures made by the reference's own code on x86-64:
+  1e-4 absolute (bitwise where the two C libraries agree).
+"""
+import numpy as np
+import pytest
+
+import simplewinderosion_gb300 as swe
+from oracle import oracle
+from simplewinderosion_gb300 import terrain
+from tests.conftest import WIND_101, bits, golden
+
+pytestmark = pytest.mark.gpu
+
+
+def world_like(port, seed=1, **kw):
+    w = swe.World(port.nx, port.nz, params=swe.Params(**kw), seed=seed)
+    return w
+
+
+def _terrain(n, seed):
+    return (terrain.normalise(terrain.fbm(n, n, seed, 4.0 / n)) + 0.1).astype(np.float32)
+
+
+def rel_close(got, want, tol=1e-5):
+    return np.abs(got.astype(np.float64) - want) <= tol * np.maximum(1.0, np.abs(want.astype(np.float64)))
+
+
+def test_normals_bitwise():
+    n = 40
+    rs = np.random.RandomState(3)
+    h = rs.uniform(0, 0.5, (n, n + 7)).astype(np.float32)
+    h[:9, :9] = 0.25
+    h[20:, :] += 0.3
+    port = oracle.Port(n, n + 7)
+    port.set_field(0, h)
+    w = swe.World(n, n + 7)
+    w.upload(swe.Field.HEIGHT, h)
+    assert np.array_equal(bits(w.normals()), bits(port.normals()))
+
+
+def test_normals_golden():
+    g = golden("normals_16")
+    w = swe.World(16)
+    w.upload(swe.Field.HEIGHT, g["height"])
+    assert np.array_equal(bits(w.normals()), bits(g["normals"]))
+
+
+def test_cascade_golden_sequence():
+    g = golden("cascade_12")
+    w = swe.World(16)
+    w.upload(swe.Field.HEIGHT, g["height"])
+    for (x, z), after in zip(g["cells"], g["after"]):
+        w.cascade(int(x), int(z))
+        assert np.array_equal(bits(w.height), bits(after)), (x, z)
+
+
+def test_device_expf_equals_c_library_everywhere():
+    # every float argument with a finite non-zero result: [-104, 0] and [0, 88.8]
+    w = swe.World(8)
+    ranges = [(0x80000000, int(np.float32(-104.0).view(np.uint32)) + 1),
+              (0x00000000, int(np.float32(88.8).view(np.uint32)) + 1)]
+    chunk = 1 << 26
+    bad = 0
+    for lo, hi in ranges:
+        for a in range(lo, hi, chunk):
+            n = min(chunk, hi - a)
+            got = w.expf_bits(a, n)
+            want = oracle.expf_libm_bits(a, n)
+            same = (bits(got) == bits(want)) | (np.isnan(got) & np.isnan(want))
+            bad += int((~same).sum())
+    assert bad == 0
+
+
+@pytest.mark.parametrize("wind", [(1.0, 0.0, 0.0), WIND_101])
+def test_trace_bitwise_vs_port(wind):
+    n, count, steps = 128, 512, 513
+    h = _terrain(n, 5)
+    rs = np.random.RandomState(9)
+    spawn = (rs.randint(0, n, (count, 2)) + rs.randint(0, 1000, (count, 2)) / np.float32(1000)).astype(np.float32)
+    tape = rs.randint(0, 2**31 - 1, (count, steps, 3)).astype(np.int32)
+    port = oracle.Port(n, pspeed=wind)
+    port.set_field(0, h)
+    w = swe.World(n, params=swe.Params(pspeed=wind))
+    w.upload(swe.Field.HEIGHT, h)
+    got = w.trace(spawn, steps, tape)
+    assert np.array_equal(bits(got), bits(port.trace(spawn, steps, tape)))
+
+
+def test_trace_vs_reference_semantics_1e5():
+    # check (a): 1000 particles x 513 steps on the 256^2 map of the small config
+    n, count, steps = 256, 1000, 513
+    h = terrain.config_plain_small(seed=1, n=n)
+    rs = np.random.RandomState(11)
+    spawn = (rs.randint(0, n, (count, 2)) + rs.randint(0, 1000, (count, 2)) / np.float32(1000)).astype(np.float32)
+    tape = rs.randint(0, 2**31 - 1, (count, steps, 3)).astype(np.int32)
+    port = oracle.Port(n, exp_kind=oracle.EXP_LIBM, pspeed=WIND_101)
+    port.set_field(0, h)
+    want = port.trace(spawn, steps, tape)
+    w = swe.World(n, params=swe.Params(pspeed=WIND_101))
+    w.upload(swe.Field.HEIGHT, h)
+    got = w.trace(spawn, steps, tape)
+    assert np.array_equal(got[..., :2], want[..., :2])  # alive flags and ages agree exactly
+    ok = rel_close(got[..., 2:], want[..., 2:])
+    assert ok.all(), f"{(~ok).sum()} of {ok.size} values outside 1e-5 (max {np.abs(got - want).max()})"
+    print(f"trace 256^2: {np.mean(bits(got) == bits(want)):.6f} of values bit-identical")
+
+
+@pytest.mark.parametrize("name", ["trace_48_default", "trace_48_wind101"])
+def test_trace_vs_reference_golden(name):
+    g = golden(name)
+    rec = g["records"]
+    count, steps = rec.shape[:2]
+    tape = np.random.RandomState(int(g["tape_seed"]) + 1000).randint(0, 2**31 - 1, size=(count, steps, 3)).astype(np.int32)
+    w = swe.World(48, params=swe.Params(pspeed=tuple(float(v) for v in g["pspeed"])))
+    w.upload(swe.Field.HEIGHT, g["height"])
+    got = w.trace(g["spawn"], steps, tape)
+    assert np.array_equal(got[..., :2], rec[..., :2])
+    assert rel_close(got[..., 2:], rec[..., 2:]).all()
+
+
+def test_fly_live_bitwise():
+    n, steps = 64, 520
+    h = _terrain(n, 6)
+    tape = np.random.RandomState(6).randint(0, 2**31 - 1, (steps, 3)).astype(np.int32)
+    port = oracle.Port(n, pspeed=WIND_101)
+    port.set_field(0, h)
+    w = swe.World(n, params=swe.Params(pspeed=WIND_101))
+    w.upload(swe.Field.HEIGHT, h)
+    for x, z in [(3.2, 4.7), (10.5, 20.499), (0.0, 63.4), (40.0, 2.0)]:
+        a, oka = port.fly_live(x, z, steps, tape)
+        b, okb = w.fly(x, z, steps, tape)
+        assert oka == okb
+        assert np.array_equal(bits(a), bits(b))
+        for f in swe.FIELDS:
+            assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), f
+
+
+@pytest.mark.parametrize("n,particles,cycles,wind", [(16, 40, 5, (0.0, 0.0, -1.0)), (64, 200, 3, WIND_101),
+                                                     (96, 300, 2, (1.0, 0.0, 0.0))])
+def test_ordered_erode_bitwise_vs_port(n, particles, cycles, wind):
+    h = _terrain(n, n)
+    port = oracle.Port(n, pspeed=wind)
+    port.set_field(0, h)
+    port.seed(123)
+    port.erode(particles, cycles)
+    w = swe.World(n, params=swe.Params(pspeed=wind), seed=123)
+    w.upload(swe.Field.HEIGHT, h)
+    w.erode(particles, cycles, mode=swe.Mode.ORDERED)
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), f
+    assert w.stats() == port.stats()
+
+
+@pytest.mark.parametrize("name", ["erode_32_default", "erode_64_wind101", "erode_16_edges"])
+def test_ordered_erode_vs_reference_golden(name):
+    g = golden(name)
+    n = int(g["n"])
+    w = swe.World(n, params=swe.Params(pspeed=tuple(float(v) for v in g["pspeed"])), seed=int(g["seed"]))
+    w.upload(swe.Field.HEIGHT, g["height0"])
+    w.erode(int(g["particles"]), int(g["cycles"]), mode=swe.Mode.ORDERED)
+    got = np.stack([w.download(f) for f in swe.FIELDS])
+    assert np.allclose(got, g["fields"], atol=1e-4, rtol=0), np.abs(got - g["fields"]).max()
+    print(f"{name}: {np.mean(bits(got) == bits(g['fields'])):.6f} of values bit-identical to the reference")
+
+
+def test_ordered_erode_100_cycles_vs_reference_semantics():
+    # check (b): small config, 256^2, 100 cycles x 1000 particles, wind (1,0,1)
+    n = 256
+    h = terrain.config_plain_small(seed=1, n=n)
+    port = oracle.Port(n, exp_kind=oracle.EXP_LIBM, pspeed=WIND_101)
+    port.set_field(0, h)
+    port.seed(2024)
+    port.erode(1000, 100)
+    w = swe.World(n, params=swe.Params(pspeed=WIND_101), seed=2024)
+    w.upload(swe.Field.HEIGHT, h)
+    w.erode(1000, 100, mode=swe.Mode.ORDERED)
+    got, want = w.height, port.get_field(0)
+    err = np.abs(got - want).max()
+    print(f"ordered 100 cycles: max |dh| {err:.3g}, bit-identical cells {np.mean(bits(got) == bits(want)):.6f}")
+    assert err <= 1e-4
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), f
+
+
+def test_ordered_tape_equals_replica():
+    n = 32
+    h = _terrain(n, 2)
+    tape = oracle.glibc_rand_sequence(77, 200000)
+    a = swe.World(n, seed=77)
+    a.upload(swe.Field.HEIGHT, h)
+    a.erode(50, 2, mode=swe.Mode.ORDERED)
+    b = swe.World(n, seed=1)
+    b.upload(swe.Field.HEIGHT, h)
+    b.set_rand_tape(tape)
+    b.erode(50, 2, mode=swe.Mode.ORDERED)
+    assert np.array_equal(bits(a.height), bits(b.height))
+
+
+def test_ordered_tape_exhaustion_is_reported():
+    w = swe.World(16, seed=1)
+    w.upload(swe.Field.HEIGHT, _terrain(16, 1))
+    w.set_rand_tape(np.arange(10, dtype=np.int32))
+    with pytest.raises(swe.SweError) as e:
+        w.erode(20, 1, mode=swe.Mode.ORDERED)
+    assert e.value.code == -3
+    w.sync()  # status was cleared

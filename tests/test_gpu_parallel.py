@@ -1,0 +1,126 @@
+"""CUDA parallel fixed-point mode against its CPU model (bit for bit), plus
+its invariants: exact mass conservation, determinism, graph reuse, split
+calls, and device-side status reporting."""
+import numpy as np
+import pytest
+
+import simplewinderosion_gb300 as swe
+from oracle import oracle
+from simplewinderosion_gb300 import terrain
+from tests.conftest import WIND_101, bits
+
+pytestmark = pytest.mark.gpu
+
+
+def _terrain(nx, nz, seed):
+    return (terrain.normalise(terrain.fbm(nx, nz, seed, 4.0 / max(nx, nz))) + 0.1).astype(np.float32)
+
+
+def _pair(nx, nz, seed, wind=WIND_101, frac_bits=24, wseed=5):
+    h = _terrain(nx, nz, seed)
+    port = oracle.Port(nx, nz, pspeed=wind, frac_bits=frac_bits)
+    port.set_field(0, h)
+    w = swe.World(nx, nz, params=swe.Params(pspeed=wind, frac_bits=frac_bits), seed=wseed)
+    w.upload(swe.Field.HEIGHT, h)
+    return port, w
+
+
+@pytest.mark.parametrize("nx,nz,particles,cycles,wind,frac_bits", [
+    (16, 16, 64, 3, WIND_101, 24),
+    (33, 70, 900, 2, (0.0, 0.0, -1.0), 24),
+    (64, 64, 4096, 2, WIND_101, 16),
+    (96, 64, 6144, 2, (1.0, 0.0, 0.0), 28),
+    (128, 128, 16384, 2, WIND_101, 24),
+])
+def test_parallel_bitwise_vs_cpu_model(nx, nz, particles, cycles, wind, frac_bits):
+    port, w = _pair(nx, nz, 7, wind, frac_bits)
+    port.par_erode(particles, cycles, seed=5)
+    w.erode(particles, cycles, mode=swe.Mode.PARALLEL)
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), f
+    m, e = port.par_ledger()
+    assert w.mass_ledger() == (m, 0, e)
+    assert w.stats() == port.stats()
+
+
+def test_parallel_conserves_mass_exactly_256():
+    n = 256
+    h = terrain.config_plain_small(seed=1, n=n)
+    w = swe.World(n, params=swe.Params(pspeed=WIND_101), seed=9)
+    w.upload(swe.Field.HEIGHT, h)
+    m0, _, e0 = w.mass_ledger()
+    assert e0 == 0
+    for _ in range(3):
+        w.erode(n * n, 2, mode=swe.Mode.PARALLEL)
+        m, i, e = w.mass_ledger()
+        assert i == 0 and m + e == m0
+    steps, spawned, transfers = w.stats()
+    assert spawned == 2 * n * n and steps > spawned and transfers > 0
+
+
+def test_parallel_deterministic():
+    n = 256
+    h = terrain.config_plain_small(seed=2, n=n)
+    out = []
+    for _ in range(2):
+        w = swe.World(n, params=swe.Params(pspeed=WIND_101), seed=4)
+        w.upload(swe.Field.HEIGHT, h)
+        w.erode(n * n, 3, mode=swe.Mode.PARALLEL)
+        out.append([w.download(f) for f in swe.FIELDS])
+    for a, b in zip(*out):
+        assert np.array_equal(bits(a), bits(b))
+
+
+def test_parallel_split_calls_and_graph_reuse():
+    port, w = _pair(48, 48, 3)
+    w.erode(500, 2, mode=swe.Mode.PARALLEL)
+    w.erode(800, 1, mode=swe.Mode.PARALLEL)   # new graph for a new particle count
+    w.erode(500, 1, mode=swe.Mode.PARALLEL)
+    cyc = port.par_erode(500, 2, seed=5)
+    cyc = port.par_erode(800, 1, seed=5, cycle=cyc)
+    port.par_erode(500, 1, seed=5, cycle=cyc)
+    assert np.array_equal(bits(port.get_field(0)), bits(w.height))
+
+
+def test_modes_interleave_through_float_heights():
+    port, w = _pair(40, 40, 4)
+    w.erode(300, 1, mode=swe.Mode.PARALLEL)
+    port.par_erode(300, 1, seed=5)
+    h = w.height
+    assert np.array_equal(bits(h), bits(port.get_field(0)))
+    w.erode(30, 1, mode=swe.Mode.ORDERED)  # float path continues from the converted map
+    assert np.isfinite(w.height).all()
+
+
+def test_zero_particles_and_zero_cycles():
+    port, w = _pair(20, 20, 5)
+    w.erode(0, 2, mode=swe.Mode.PARALLEL)
+    port.par_erode(0, 2, seed=5)
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f)))
+    w.erode(100, 0, mode=swe.Mode.PARALLEL)
+    assert w.stats() == (0, 0, 0)
+
+
+def test_nonfinite_height_is_reported_not_faulted():
+    w = swe.World(32)
+    h = _terrain(32, 32, 1)
+    h[5, 5] = np.nan
+    w.upload(swe.Field.HEIGHT, h)
+    with pytest.raises(swe.SweError) as e:
+        w.erode(100, 1, mode=swe.Mode.PARALLEL)
+    assert e.value.code == -3
+    assert "range" in str(e.value)
+    w.upload(swe.Field.HEIGHT, _terrain(32, 32, 1))
+    w.erode(100, 1, mode=swe.Mode.PARALLEL)  # the world stays usable
+
+
+def test_upload_download_roundtrip_every_field():
+    w = swe.World(17, 29)
+    rs = np.random.RandomState(0)
+    for f in swe.FIELDS:
+        a = rs.standard_normal((17, 29)).astype(np.float32)
+        w.upload(f, a)
+        assert np.array_equal(bits(w.download(f)), bits(a))
+    with pytest.raises(swe.SweError):
+        w.upload(swe.Field.HEIGHT, np.zeros(10, np.float32))
