@@ -1,0 +1,406 @@
+"""Benchmark: erode cycles/s of the GB300 parallel erosion path at 1024^2.
+
+Workload (the plain-method configuration at 1024^2): a 1024x1024 FP32 height
+map of seeded fBm (improved Perlin noise, base frequency 1/256, 8 octaves,
+in [0, 0.5]) plus a 0.1 +- 0.02 sediment layer and a square bedrock pyramid
+(height 0.4, base 200 cells) at the centre; prevailing wind
+normalize(1,0,1); 1,048,576 particles per erode cycle; parallel fixed-point
+mode with int32 Q16.16 heights. One bench step = one erode cycle
+(World::erode(P), source/world.hpp:36-77). Synthetic seeded data.
+
+Timing: W untimed warm-up cycles, then K cycles, each bracketed by CUDA
+events on the world's stream; L2 is flushed (256 MiB write) before every
+timed cycle, outside the events. Multi-GPU (torchrun): one independent
+replica world per rank (the map does not shard), barrier + max over ranks.
+
+Also reported: kernel roofline (fly + cascade kernels, CUDA events inside
+the cycle graph), a CPU baseline (the oracle, bounded sample, one core),
+end-to-end cycles/s through the C ABI with pinned host buffers, and clocks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "erode cycles/s at 1024^2 (parallel GPU mode)"
+UNIT = "cycles/s"
+L2_FLUSH_BYTES = 256 << 20
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--particles", type=int, default=0, help="particles per cycle (default size^2)")
+    ap.add_argument("--frac-bits", type=int, default=16)
+    ap.add_argument("--cpu-sample", type=int, default=65536, help="particles in the CPU baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(size: int):
+    import simplewinderosion_gb300 as swe
+    from simplewinderosion_gb300 import terrain
+    h = terrain.config_plain_large(seed=2, n=size)
+    wind = swe.wind_direction(1.0, 0.0, 1.0)
+    return h, wind
+
+
+def config_dict(args, particles):
+    return {
+        "workload": f"plain method {args.size}^2: fBm(1/256)+sediment+pyramid(0.4, base 200), "
+                    f"{particles} particles/cycle, wind normalize(1,0,1), parallel fixed-point "
+                    f"int32 Q{32 - args.frac_bits}.{args.frac_bits}",
+        "map": f"{args.size}x{args.size}",
+        "particles_per_cycle": particles,
+        "max_age": 512,
+        "frac_bits": args.frac_bits,
+        "l2": "flushed (256 MiB write) before every timed cycle",
+        "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+    }
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self._t:
+                self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_cores_desc() -> str:
+    return f"{platform.machine()} x{os.cpu_count()}"
+
+
+def cpu_sample(size: int, h, wind, particles: int, total_particles: int, prefer_reference: bool):
+    """Time `particles` particles of one World::erode call on the CPU with the
+    reference's own code when it is compiled here (oracle/_ref), else the
+    oracle port; return (cycles/s, kind, seconds, particle-steps)."""
+    from oracle import oracle
+    kind = "port"
+    if prefer_reference and oracle.reference_available():
+        try:
+            oracle.build_reference(sizes=(size,))
+            kind = "reference"
+        except Exception:
+            kind = "port"
+    if kind == "reference":
+        ref = oracle.Reference(size)
+        ref.reset(h)
+        ref.srand(1)
+        t0 = time.perf_counter()
+        ref.erode(particles, 1, pspeed=wind)
+        dt = time.perf_counter() - t0
+        steps = None
+    else:
+        port = oracle.Port(size, pspeed=wind)
+        port.set_field(0, h)
+        port.seed(1)
+        t0 = time.perf_counter()
+        port.erode(particles, 1)
+        dt = time.perf_counter() - t0
+        steps = port.stats()[0]
+    cycles_per_s = particles / (dt * total_particles)
+    return cycles_per_s, kind, dt, steps
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    size = args.size
+    particles = args.particles or size * size
+    h, wind = workload(size)
+    sample = args.ref_sample
+    vals, secs, kind = [], [], "port"
+    for i in range(args.warmup + args.steps):
+        v, kind, dt, _ = cpu_sample(size, h, wind, sample, particles, prefer_reference=True)
+        if i >= args.warmup:
+            vals.append(v)
+            secs.append(dt)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 / value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": config_dict(args, particles),
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": f"{sample} of {particles} particles of one sequential World::erode cycle per step on "
+                      f"{cpu_cores_desc()} (the reference loop is single-threaded), scaled to cycles/s",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import simplewinderosion_gb300 as swe
+
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world_size > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    size = args.size
+    particles = args.particles or size * size
+    h, wind = workload(size)
+    params = swe.Params(pspeed=wind, frac_bits=args.frac_bits)
+    w = swe.World(size, params=params, seed=1000 + rank)
+    w.upload(swe.Field.HEIGHT, h)
+    stream = torch.cuda.ExternalStream(w.stream(), device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    for _ in range(args.warmup):
+        w.erode(particles, 1, mode=swe.Mode.PARALLEL)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    if world_size > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    fly_ms = cas_ms = 0.0
+    psteps = transfers = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.erode(particles, 1, mode=swe.Mode.PARALLEL, sync=False)
+        e1.record(stream)
+        w.sync()
+        total_ms += e0.elapsed_time(e1)
+        f, c = w.kernel_times()
+        fly_ms += f
+        cas_ms += c
+        s, _, t = w.stats()
+        psteps += s
+        transfers += t
+    torch.cuda.synchronize()
+    if world_size > 1:
+        dist.barrier()
+        tmax = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        total_ms = float(tmax.item())
+    clocks = sampler.stop() if sampler else None
+
+    cycles_total = args.steps * world_size
+    value = cycles_total / (total_ms / 1e3)
+    ms_per_step = total_ms / args.steps
+
+    # Roofline of the step kernels (fly + cascade passes): algorithmic bytes
+    # per particle-step B = 76 + 16 k (3x3 height gather 36, four track
+    # read-modify-writes 32, the cell's exchange read-modify-write 8, 16 per
+    # cascade transfer), k = transfers per particle-step.
+    k = transfers / max(psteps, 1)
+    bytes_per_step = 76.0 + 16.0 * k
+    kernel_ms = fly_ms + cas_ms
+    achieved = bytes_per_step * psteps / (kernel_ms / 1e3) / 1e9
+    peak, peak_note = FALLBACK_HBM_GBS, "fallback"
+    try:
+        peak = float(json.loads(PEAKS_FILE.read_text())["hbm_gbs"])
+        peak_note = "measured"
+    except Exception:
+        pass
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            tj = json.loads(tfile.read_text())
+            traffic = tj.get("bytes_per_particle_step", None)
+            if traffic is not None:
+                traffic = traffic * psteps / args.steps
+        except Exception:
+            traffic = None
+
+    per_cycle_launches = 2 + (params.max_age + 2) * (1 + 4)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world_size,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+i32",
+        "data": "synthetic",
+        "config": config_dict(args, particles),
+        "particle_steps_per_s": psteps * world_size / (total_ms / 1e3),
+        "kernels": {"fly_ms_per_cycle": fly_ms / args.steps, "cascade_ms_per_cycle": cas_ms / args.steps,
+                    "k_transfers_per_step": k, "particle_steps_per_cycle": psteps / args.steps},
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "step kernels k_par_fly + k_par_cascade",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "peak_source": peak_note,
+            "bytes_per_particle_step": bytes_per_step,
+            "traffic": traffic,
+        },
+        "gpu_launches": per_cycle_launches * args.steps,
+        "clocks": clocks,
+    }
+
+    if not args.no_e2e:
+        line["e2e"] = e2e(w, swe, torch, stream, h, particles, args, world_size)
+
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
+        v, kind, dt, steps = cpu_sample(size, h, wind, args.cpu_sample, particles, prefer_reference=True)
+        line["cpu_baseline"] = {
+            "value": v, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": f"{args.cpu_sample} of {particles} particles of one sequential World::erode cycle "
+                      f"({dt:.1f} s on {cpu_cores_desc()}, one thread: the reference loop is sequential), "
+                      f"scaled to cycles/s",
+        }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    w.close()
+    if world_size > 1:
+        dist.destroy_process_group()
+
+
+def e2e(w, swe, torch, stream, h, particles, args, world_size):
+    """Cycles/s through the C ABI with host buffers: per cycle, upload the
+    height map from pinned memory, erode one cycle, read back height and
+    momentum (the fields the reference's app loop reads after erode,
+    SimpleWindErosion.cpp:217-230)."""
+    import torch.distributed as dist
+    n = w.n
+    h_pin = torch.from_numpy(np.ascontiguousarray(h.reshape(-1))).pin_memory()
+    outs = [torch.empty(n, dtype=torch.float32).pin_memory() for _ in range(4)]
+    fields = [swe.Field.HEIGHT, swe.Field.MOMENTUMX, swe.Field.MOMENTUMY, swe.Field.MOMENTUMZ]
+    w.upload_ptr(swe.Field.HEIGHT, h_pin.data_ptr(), n)
+    w.erode(particles, 1, mode=swe.Mode.PARALLEL)
+    torch.cuda.synchronize()
+    if world_size > 1:
+        dist.barrier()
+    total = 0.0
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.upload_ptr(swe.Field.HEIGHT, h_pin.data_ptr(), n)
+        w.erode(particles, 1, mode=swe.Mode.PARALLEL, sync=False)
+        for f, o in zip(fields, outs):
+            w.download_ptr(f, o.data_ptr(), n)
+        e1.record(stream)
+        w.sync()
+        total += e0.elapsed_time(e1)
+    if world_size > 1:
+        t = torch.tensor([total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    return {"value": args.steps * world_size / (total / 1e3), "unit": UNIT,
+            "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * 4 * n}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

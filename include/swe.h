@@ -38,6 +38,7 @@ extern "C" {
 #define SWE_STATUS_NONFINITE 0x1u  /* a particle produced NaN/Inf and was retired */
 #define SWE_STATUS_RANGE 0x2u      /* a fixed-point height left its safe range     */
 #define SWE_STATUS_TAPE 0x4u       /* an ordered-mode rand tape ran out            */
+#define SWE_STATUS_TIMEOUT 0x8u    /* a grid barrier gave up waiting; cycle aborted */
 
 /* Simulation constants; swe_params_default() gives the reference's values.
  * Replaces the statics Wind::maxAge/boundarylayer/suspension/gravity
@@ -73,14 +74,16 @@ typedef enum swe_field {
 /* How World::erode's particles are run.
  *  ORDERED:  particles one after another, exactly as the reference
  *            (world.hpp:47-67), with the C library rand() sequence of
- *            srand(seed) (or a caller tape). One GPU thread; a parity mode.
- *  PARALLEL: all particles of a cycle fly together in lock-step steps. Each
- *            step reads the height map as it was at the start of the step;
- *            deposits, erosion and cascade transfers are added with integer
- *            atomics in fixed point, so mass is conserved exactly and the
- *            result does not depend on thread scheduling. Random numbers come
- *            from a counter-based generator keyed by (seed, cycle, particle,
- *            step). The throughput mode. */
+ *            srand(seed) (or a caller tape) and the C library's expf: the
+ *            reference's results bit for bit. One GPU thread; a parity mode.
+ *  PARALLEL: all particles of a cycle fly together in lock-step steps. In a
+ *            step every particle flies against the heights as they were at
+ *            the start of the step and adds its erosion/deposition to the
+ *            map in fixed point; then the cascades the step owes run in a
+ *            fixed conflict-free order (nine cell colours x%3, z%3). Mass is
+ *            conserved exactly and the result does not depend on thread
+ *            scheduling. Random numbers come from a counter-based generator
+ *            keyed by (seed, cycle, particle, step). The throughput mode. */
 typedef enum swe_mode { SWE_MODE_ORDERED = 0, SWE_MODE_PARALLEL = 1 } swe_mode;
 
 typedef struct swe_world swe_world;
@@ -162,6 +165,28 @@ int swe_world_cascade_at(swe_world* w, int x, int z);
  * map::normal calls it (cellpool.h:478-480): 3*nx*nz floats (x,y,z per cell)
  * written to host_out. */
 int swe_world_normals(swe_world* w, float* host_out, size_t n);
+
+/* The CUDA stream (a cudaStream_t) the world enqueues its work on, and a
+ * way to replace it with the caller's stream (NULL: back to a private
+ * stream). The world does not destroy a caller's stream. */
+int swe_world_get_stream(swe_world* w, void** stream);
+int swe_world_set_stream(swe_world* w, void* stream);
+
+/* Time the parallel mode spent in its fly phases and in its cascade phases
+ * (ms, the device's global timer read by one thread at the phase barriers),
+ * summed over the cycles of the last swe_world_erode call. No reference
+ * counterpart (the reference has no timing). */
+int swe_world_kernel_times(swe_world* w, double* fly_ms, double* cascade_ms);
+
+/* The same clock per phase of the parallel cycle kernel, ms summed over the
+ * last swe_world_erode call, in the order: spawn, fly, (unused), colour 0..8,
+ * ema (n <= 13 values written). */
+int swe_world_phase_times(swe_world* w, double* ms, int n);
+
+/* Cascade work of the last parallel swe_world_erode call: World::cascade
+ * evaluations, cell-steps that owed cascades, and the most cascades one cell
+ * ran in one step. */
+int swe_world_cascade_stats(swe_world* w, int64_t* cascades, int64_t* cells, int* max_iters);
 
 /* The exponential the exact-semantics kernels use (the reference's
  * std::exp(float), wind.hpp:50, i.e. this machine's C library expf,

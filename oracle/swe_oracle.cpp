@@ -483,21 +483,20 @@ void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out) {
 
 // ============================================================================
 // Part 2: CPU model of the parallel fixed-point mode. Same definitions as the
-// CUDA kernels (simplewinderosion_gb300/csrc/swe_parallel.cu). One step:
+// CUDA kernel (simplewinderosion_gb300/csrc/swe_parallel.cu). One step:
 //   fly     every live particle runs Wind::fly against the heights as they
 //           were at the start of the step; its exchange with its cell goes
-//           into a delta map D and its cell's visit count into C (integers).
-//   cascade four passes over 32x32 tiles, tile colour (tx%2, tz%2). A tile
-//           works on its cells and a one-cell halo: heights + D; then for the
-//           nine cell colours (x%3, z%3) in order, every cell with C > 0
-//           runs World::cascade C times on the current heights; halo cells
-//           go back without their D, own cells absorb theirs.
-// Same-colour tiles and same-colour cells touch disjoint 3x3 neighbourhoods,
-// so each pass is free of conflicts and the order of the whole step is fixed.
+//           into a delta map D and its cell's owed cascade into a visit map C
+//           (integers).
+//   apply   H += D for every cell.
+//   cascade for the nine cell colours (x%3, z%3) in order, every cell with
+//           C > 0 runs World::cascade up to C times on the current heights
+//           (stopping early once a cascade moves nothing: repeating it could
+//           not change anything). Cells of one colour touch disjoint 3x3
+//           neighbourhoods, so each colour is free of conflicts and the order
+//           of the whole step is fixed.
 // ============================================================================
 namespace {
-
-constexpr int kTile = 32;
 
 int32_t to_fixed(float v) {
   if (v != v) return 0;
@@ -602,31 +601,36 @@ bool par_fly(ParCtx& X, PState& P, int step) {
   return true;
 }
 
-// World::cascade in fixed point on a local height buffer (row stride ls):
-// in-bounds neighbours in the reference's order, stable descending by
-// height, each moving half the excess over the slope limit.
-int cascade_q(int32_t* L, int ls, int li, int lj, bool vx0, bool vx2, bool vz0, bool vz2, const so_params& c,
-              float scale, float inv) {
+// World::cascade in fixed point at cell (x, z) of the map H: in-bounds
+// neighbours in the reference's order, stable descending by height, each
+// moving half the excess over the slope limit. Returns the number of
+// transfers that moved a non-zero amount.
+int cascade_q(so_world* w, int32_t* H, int x, int z, float scale, float inv) {
+  const so_params& c = w->p;
+  const int nx = w->nx, nz = w->nz;
   struct K { int k; int32_t key; };
-  const bool val[8] = {vx0 && vz0, vx0, vx0 && vz2, vz0, vz2, vx2 && vz0, vx2, vx2 && vz2};
   K sn[8];
   int num = 0;
-  for (int k = 0; k < 8; k++)
-    if (val[k]) sn[num++] = K{k, L[(li + NB_DX[k]) * ls + (lj + NB_DZ[k])]};
+  for (int k = 0; k < 8; k++) {
+    const int qx = x + NB_DX[k], qz = z + NB_DZ[k];
+    if (qx < 0 || qz < 0 || qx >= nx || qz >= nz) continue;
+    sn[num++] = K{k, H[(long)qx * nz + qz]};
+  }
   insertion_sort_desc(sn, num, [](const K& a, const K& b) { return a.key > b.key; });
-  int32_t& hc = L[li * ls + lj];
+  int32_t& hc = H[(long)x * nz + z];
   int t = 0;
   for (int r = 0; r < num; r++) {
     const int k = sn[r].k;
     const float dx = (float)NB_DX[k], dz = (float)NB_DZ[k];
     const float d = std::sqrt(dx * dx + dz * dz);
-    const int64_t dq = (int64_t)hc - (int64_t)sn[r].key;
+    const int32_t dq = wsub(hc, sn[r].key);
     if (dq == 0) continue;
     const float excess = std::fabs((float)dq * inv) - d * c.maxdiff;
     if (excess <= 0.0f) continue;
-    const int32_t tq = to_fixed(c.settling * excess / 2.0f * scale);
+    const int32_t tq = to_fixed(c.settling * excess * 0.5f * scale);
+    if (tq == 0) continue;
     const int32_t sgn = dq > 0 ? tq : -tq;
-    int32_t& hn = L[(li + NB_DX[k]) * ls + (lj + NB_DZ[k])];
+    int32_t& hn = H[(long)(x + NB_DX[k]) * nz + (z + NB_DZ[k])];
     hc = wsub(hc, sgn);
     hn = wadd(hn, sgn);
     t++;
@@ -634,44 +638,24 @@ int cascade_q(int32_t* L, int ls, int li, int lj, bool vx0, bool vx2, bool vz0, 
   return t;
 }
 
-// One tile's share of a cascade pass.
-int64_t cascade_tile(so_world* w, int32_t* H, int32_t* D, int32_t* C, int tx, int tz) {
+// The cascade phase of one step: nine colours, each cell's owed cascades.
+int64_t cascade_phase(so_world* w, int32_t* H, int32_t* C) {
   const int nx = w->nx, nz = w->nz;
-  const int x0 = tx * kTile, z0 = tz * kTile;
-  const int ls = kTile + 2;
-  int32_t L[(kTile + 2) * (kTile + 2)];
   const float scale = (float)(1u << w->p.frac_bits);
   const float inv = 1.0f / scale;
-  for (int i = 0; i < ls; i++)
-    for (int j = 0; j < ls; j++) {
-      const int x = x0 + i - 1, z = z0 + j - 1;
-      L[i * ls + j] = (x >= 0 && z >= 0 && x < nx && z < nz) ? wadd(H[(long)x * nz + z], D[(long)x * nz + z]) : 0;
-    }
   int64_t transfers = 0;
-  for (int a = 0; a < 3; a++)
-    for (int b = 0; b < 3; b++)
-      for (int i = 0; i < kTile; i++)
-        for (int j = 0; j < kTile; j++) {
-          const int x = x0 + i, z = z0 + j;
-          if (x >= nx || z >= nz || x % 3 != a || z % 3 != b) continue;
-          const int cnt = C[(long)x * nz + z];
-          for (int r = 0; r < cnt; r++)
-            transfers += cascade_q(L, ls, i + 1, j + 1, x > 0, x + 1 < nx, z > 0, z + 1 < nz, w->p, scale, inv);
-        }
-  for (int i = 0; i < ls; i++)
-    for (int j = 0; j < ls; j++) {
-      const int x = x0 + i - 1, z = z0 + j - 1;
-      if (x < 0 || z < 0 || x >= nx || z >= nz) continue;
-      const long g = (long)x * nz + z;
-      const bool own = i >= 1 && j >= 1 && i <= kTile && j <= kTile;
-      if (own) {
-        H[g] = L[i * ls + j];
-        D[g] = 0;
+  for (int col = 0; col < 9; col++)
+    for (int x = col / 3; x < nx; x += 3)
+      for (int z = col % 3; z < nz; z += 3) {
+        const long g = (long)x * nz + z;
+        const int cnt = C[g];
         C[g] = 0;
-      } else {
-        H[g] = wsub(L[i * ls + j], D[g]);
+        for (int r = 0; r < cnt; r++) {
+          const int t = cascade_q(w, H, x, z, scale, inv);
+          if (t == 0) break;
+          transfers += t;
+        }
       }
-    }
   return transfers;
 }
 
@@ -694,7 +678,6 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
   const size_t n = (size_t)w->nx * w->nz;
   const float inv = 1.0f / (float)(1u << w->p.frac_bits);
   const float lrate = w->p.lrate;
-  const int ntx = (w->nx + kTile - 1) / kTile, ntz = (w->nz + kTile - 1) / kTile;
   std::vector<int64_t> tq[4];
   for (auto& t : tq) t.assign(n, 0);
   std::vector<int32_t> D(n, 0), C(n, 0);
@@ -730,11 +713,14 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
         if (par_fly(X, P, step)) next.push_back(P);
         else X.exported += P.sed_q;
       }
-      if (!next.empty())
-        for (int color = 0; color < 4; color++)
-          for (int tx = color >> 1; tx < ntx; tx += 2)
-            for (int tz = color & 1; tz < ntz; tz += 2)
-              X.transfers += cascade_tile(w, w->hq.data(), D.data(), C.data(), tx, tz);
+      if (!next.empty()) {
+        int32_t* H = w->hq.data();
+        for (size_t i = 0; i < n; i++) {
+          H[i] = wadd(H[i], D[i]);
+          D[i] = 0;
+        }
+        X.transfers += cascade_phase(w, H, C.data());
+      }
       live.swap(next);
     }
     for (size_t i = 0; i < n; i++) {

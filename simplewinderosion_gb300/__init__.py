@@ -132,6 +132,11 @@ def _setup(L):
     L.swe_world_cascade_at.argtypes = [_P, ctypes.c_int, ctypes.c_int]
     L.swe_world_normals.argtypes = [_P, _P, ctypes.c_size_t]
     L.swe_world_expf_bits.argtypes = [_P, ctypes.c_uint32, ctypes.c_size_t, _P]
+    L.swe_world_get_stream.argtypes = [_P, ctypes.POINTER(_P)]
+    L.swe_world_set_stream.argtypes = [_P, _P]
+    L.swe_world_kernel_times.argtypes = [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    L.swe_world_phase_times.argtypes = [_P, _P, ctypes.c_int]
+    L.swe_world_cascade_stats.argtypes = [_P, _i64p, _i64p, ctypes.POINTER(ctypes.c_int)]
     L.swe_last_error.restype = ctypes.c_char_p
     L.swe_last_error.argtypes = []
 
@@ -285,6 +290,45 @@ class World:
 
     def cascade(self, x: int, z: int) -> None:
         _check(lib.swe_world_cascade_at(self._h, int(x), int(z)))
+
+    # -- streams and timing
+    def stream(self) -> int:
+        p = _P()
+        _check(lib.swe_world_get_stream(self._h, ctypes.byref(p)))
+        return int(p.value or 0)
+
+    def set_stream(self, stream: int | None) -> None:
+        _check(lib.swe_world_set_stream(self._h, _P(stream) if stream else None))
+
+    def kernel_times(self) -> tuple[float, float]:
+        """(fly_ms, cascade_ms) of the parallel mode, summed over the cycles
+        of the last erode call."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(lib.swe_world_kernel_times(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    PHASES = ["spawn", "fly", "unused"] + [f"colour{k}" for k in range(9)] + ["ema"]
+
+    def cascade_stats(self) -> tuple[int, int, int]:
+        """(cascade evaluations, cell-steps with owed cascades, max cascades
+        of one cell in one step) of the last parallel erode call."""
+        a, b, m = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        _check(lib.swe_world_cascade_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(m)))
+        return a.value, b.value, m.value
+
+    def phase_times(self) -> dict:
+        """Per-phase time (ms) of the parallel cycle kernel over the last
+        erode call."""
+        out = np.zeros(13, dtype=np.float64)
+        _check(lib.swe_world_phase_times(self._h, _ptr(out), 13))
+        return dict(zip(self.PHASES, out.tolist()))
+
+    def upload_ptr(self, f: Field, host_ptr: int, n: int) -> None:
+        """Upload from a raw host pointer (e.g. pinned memory)."""
+        _check(lib.swe_world_upload(self._h, int(f), _P(host_ptr), n))
+
+    def download_ptr(self, f: Field, host_ptr: int, n: int) -> None:
+        _check(lib.swe_world_download(self._h, int(f), _P(host_ptr), n))
 
     def expf_bits(self, first_bits: int, n: int) -> np.ndarray:
         """The device's reference-compatible expf over n consecutive float bit

@@ -7,7 +7,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/swe.h"
+#include "swe.h"
 #include "swe_kernels.h"
 
 using swe::Consts;
@@ -92,16 +92,16 @@ struct swe_world {
   int32_t* tape = nullptr;
   long long tape_len = 0;
   // parallel mode
-  int32_t* hq = nullptr;      // 3n: heights, exchange deltas, visit counts
+  int32_t* hq = nullptr;      // heights, exchange deltas, visit counts (3 padded maps)
   long long* tq = nullptr;    // 4n
   void* pstate = nullptr;     // 2 buffers x 9 arrays x capacity
   int pcap = 0;
   swe::ParallelBuffers pb{};
   bool hq_valid = false;
-  int step_grid = 0;
+  int cycle_grid = 0;
   long long* dsum = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  int g_particles = -1;
+  swe::GridBarrier* gbar = nullptr;
+  bool own_stream = true;
   uint32_t* expf_x = nullptr;  // device copy of the expf exception list
   int8_t* expf_d = nullptr;
   int expf_n = 0;
@@ -122,11 +122,6 @@ struct swe_world {
     return c;
   }
 
-  void drop_graph() {
-    if (gexec) cudaGraphExecDestroy(gexec);
-    gexec = nullptr;
-    g_particles = -1;
-  }
 };
 
 namespace {
@@ -138,13 +133,19 @@ int use_device(swe_world* w) {
 
 // Parallel-mode buffers, grown to hold `particles`.
 int ensure_parallel(swe_world* w, int particles) {
+  // heights, exchange deltas and visit counts, each padded to 64 elements
+  // so every map starts 256-byte aligned (the apply phase uses int4).
+  const size_t stride = ((size_t)w->n + 63) & ~(size_t)63;
   if (!w->hq) {
-    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 3 * w->n));
-    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 3 * w->n, w->stream));
+    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 3 * stride));
+    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 3 * stride, w->stream));
     SWE_CK(cudaMalloc(&w->tq, sizeof(long long) * 4 * w->n));
     SWE_CK(cudaMemsetAsync(w->tq, 0, sizeof(long long) * 4 * w->n, w->stream));
     SWE_CK(cudaMalloc(&w->dsum, sizeof(long long)));
-    w->step_grid = swe::par_step_grid(w->device);
+    SWE_CK(cudaMalloc(&w->gbar, sizeof(swe::GridBarrier)));
+    SWE_CK(cudaMemsetAsync(w->gbar, 0, sizeof(swe::GridBarrier), w->stream));
+    w->cycle_grid = swe::cycle_grid(w->device);
+    if (w->cycle_grid < 1) return fail(SWE_ERR_CUDA, "device cannot run the cooperative cycle kernel");
   }
   if (particles > w->pcap || !w->pstate) {
     const int cap = particles > 0 ? particles : 1;
@@ -152,12 +153,11 @@ int ensure_parallel(swe_world* w, int particles) {
     w->pstate = nullptr;
     SWE_CK(cudaMalloc(&w->pstate, sizeof(int32_t) * 9 * 2 * (size_t)cap));
     w->pcap = cap;
-    w->drop_graph();
   }
   swe::ParallelBuffers& B = w->pb;
   B.hq = w->hq;
-  B.dq = w->hq + w->n;
-  B.visits = w->hq + 2 * w->n;
+  B.dq = w->hq + stride;
+  B.visits = w->hq + 2 * stride;
   for (int k = 0; k < 4; k++) B.tq[k] = w->tq + (size_t)k * w->n;
   int32_t* base = reinterpret_cast<int32_t*>(w->pstate);
   for (int b = 0; b < 2; b++) {
@@ -186,35 +186,12 @@ int ensure_fixed(swe_world* w) {
   return SWE_OK;
 }
 
-// Enqueue one parallel erode cycle (spawn, max_age+2 fly + cascade steps, EMA).
+// Enqueue one parallel erode cycle: reset the grid barrier, then the
+// persistent cooperative kernel (spawn, steps, EMA).
 int enqueue_parallel_cycle(swe_world* w, int particles) {
-  const Consts c = w->consts();
-  swe::launch_par_spawn(w->pb, c, w->seed, w->cnt, particles, w->n, w->stream);
-  const int nsteps = w->p.max_age + 2;
-  for (int t = 0; t < nsteps; t++) {
-    swe::launch_par_fly(w->pb, c, w->seed, w->cnt, t, w->step_grid, w->stream);
-    swe::launch_par_cascade(w->pb, c, w->cnt, t, w->stream);
-  }
-  swe::launch_par_ema(w->pb, w->F, c, w->cnt, w->n, w->stream);
-  SWE_CK(cudaGetLastError());
-  return SWE_OK;
-}
-
-int build_graph(swe_world* w, int particles) {
-  w->drop_graph();
-  cudaGraph_t g = nullptr;
-  SWE_CK(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_parallel_cycle(w, particles);
-  cudaError_t e = cudaStreamEndCapture(w->stream, &g);
-  if (rc != SWE_OK) {
-    if (g) cudaGraphDestroy(g);
-    return rc;
-  }
-  SWE_CK(e);
-  e = cudaGraphInstantiate(&w->gexec, g, 0);
-  cudaGraphDestroy(g);
-  SWE_CK(e);
-  w->g_particles = particles;
+  SWE_CK(cudaMemsetAsync(w->gbar, 0, sizeof(swe::GridBarrier), w->stream));
+  SWE_CK(swe::launch_par_cycle(w->pb, w->F, w->consts(), w->seed, w->cnt, w->gbar, particles, w->cycle_grid,
+                               w->stream));
   return SWE_OK;
 }
 
@@ -301,7 +278,6 @@ void swe_world_destroy(swe_world* w) {
   if (!w) return;
   cudaSetDevice(w->device);
   if (w->stream) cudaStreamSynchronize(w->stream);
-  w->drop_graph();
   cudaFree(w->fbase);
   cudaFree(w->cnt);
   cudaFree(w->grand);
@@ -310,9 +286,10 @@ void swe_world_destroy(swe_world* w) {
   cudaFree(w->tq);
   cudaFree(w->pstate);
   cudaFree(w->dsum);
+  cudaFree(w->gbar);
   cudaFree(w->expf_x);
   cudaFree(w->expf_d);
-  if (w->stream) cudaStreamDestroy(w->stream);
+  if (w->stream && w->own_stream) cudaStreamDestroy(w->stream);
   delete w;
 }
 
@@ -322,7 +299,6 @@ int swe_world_set_params(swe_world* w, const swe_params* p) {
   if (!params_ok(*p, why)) return fail(SWE_ERR_INVALID, why);
   if (p->frac_bits != w->p.frac_bits) w->hq_valid = false;
   w->p = *p;
-  w->drop_graph();
   return SWE_OK;
 }
 
@@ -390,10 +366,9 @@ int swe_world_erode(swe_world* w, int cycles, int particles, swe_mode mode) {
   }
   if (int rc = ensure_parallel(w, particles)) return rc;
   if (int rc = ensure_fixed(w)) return rc;
-  if (!w->gexec || w->g_particles != particles) {
-    if (int rc = build_graph(w, particles)) return rc;
-  }
-  for (int k = 0; k < cycles; k++) SWE_CK(cudaGraphLaunch(w->gexec, w->stream));
+  SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, w->stream));
+  for (int k = 0; k < cycles; k++)
+    if (int rc = enqueue_parallel_cycle(w, particles)) return rc;
   return SWE_OK;
 }
 
@@ -571,6 +546,63 @@ int swe_world_normals(swe_world* w, float* host_out, size_t n) {
   int rc = run();
   cudaFree(d_out);
   return rc;
+}
+
+int swe_world_get_stream(swe_world* w, void** stream) {
+  if (!w || !stream) return fail(SWE_ERR_INVALID, "NULL argument");
+  *stream = (void*)w->stream;
+  return SWE_OK;
+}
+
+int swe_world_set_stream(swe_world* w, void* stream) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  if (w->own_stream) SWE_CK(cudaStreamDestroy(w->stream));
+  if (stream) {
+    w->stream = (cudaStream_t)stream;
+    w->own_stream = false;
+  } else {
+    SWE_CK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    w->own_stream = true;
+  }
+  return SWE_OK;
+}
+
+int swe_world_kernel_times(swe_world* w, double* fly_ms, double* cascade_ms) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  unsigned long long t[2] = {0, 0};
+  SWE_CK(cudaMemcpyAsync(t, &w->cnt->fly_ns, sizeof(t), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  if (fly_ms) *fly_ms = (double)t[0] * 1e-6;
+  if (cascade_ms) *cascade_ms = (double)t[1] * 1e-6;
+  return SWE_OK;
+}
+
+int swe_world_phase_times(swe_world* w, double* ms, int n) {
+  if (!w || !ms) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (n < 0 || n > 13) return fail(SWE_ERR_INVALID, "n must be in [0, 13]");
+  if (int rc = use_device(w)) return rc;
+  unsigned long long t[13];
+  SWE_CK(cudaMemcpyAsync(t, w->cnt->phase_ns, sizeof(t), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  for (int k = 0; k < n; k++) ms[k] = (double)t[k] * 1e-6;
+  return SWE_OK;
+}
+
+int swe_world_cascade_stats(swe_world* w, int64_t* cascades, int64_t* cells, int* max_iters) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  unsigned long long v[2] = {0, 0};
+  unsigned int m = 0;
+  SWE_CK(cudaMemcpyAsync(v, &w->cnt->cascades, sizeof(v), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaMemcpyAsync(&m, &w->cnt->max_cascade_iters, sizeof(m), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  if (cascades) *cascades = (int64_t)v[0];
+  if (cells) *cells = (int64_t)v[1];
+  if (max_iters) *max_iters = (int)m;
+  return SWE_OK;
 }
 
 int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host_y) {

@@ -38,14 +38,12 @@ struct ParallelBuffers {
 };
 
 void launch_height_to_fixed(const float* height, int32_t* q, const Consts& c, Counters* cnt, cudaStream_t s);
-void launch_par_spawn(const ParallelBuffers& B, const Consts& c, uint64_t seed, Counters* cnt, int particles,
-                      long n_cells, cudaStream_t s);
-void launch_par_fly(const ParallelBuffers& B, const Consts& c, uint64_t seed, Counters* cnt, int step, int grid,
-                    cudaStream_t s);
-void launch_par_cascade(const ParallelBuffers& B, const Consts& c, Counters* cnt, int step, cudaStream_t s);
-void launch_par_ema(const ParallelBuffers& B, const Fields& F, const Consts& c, Counters* cnt, long n_cells,
-                    cudaStream_t s);
-int par_step_grid(int device);
+// Number of co-resident blocks of the persistent cycle kernel (0 if the
+// device cannot launch cooperative kernels).
+int cycle_grid(int device);
+// One parallel erode cycle as one cooperative kernel.
+cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
+                             Counters* cnt, GridBarrier* gb, int particles, int grid, cudaStream_t s);
 void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s);
 
 }  // namespace swe

@@ -1,33 +1,37 @@
 // Parallel fixed-point erosion: all particles of an erode cycle fly together.
 //
-// One cycle (the World::erode(P) call, world.hpp:36-77) is
-//   k_par_spawn                 zero the track accumulators, spawn P particles
-//   (k_par_fly, 4 x k_par_cascade) x (max_age + 2) steps
-//   k_par_ema                   tracks -> float, EMA of massflow/momentum
-//                               (world.hpp:70-76), fixed-point heights -> float
-//
-// Step semantics.
-//  fly      every live particle runs Wind::fly (wind.hpp:28-117) against the
-//           heights as they were at the start of the step (nothing writes H
-//           during this kernel). Its erosion/deposition exchange
-//           (wind.hpp:110-112) is added to the delta map D and the cascade it
-//           owes its cell (wind.hpp:114) to the visit map C, with integer
-//           atomics.
-//  cascade  World::cascade (world.hpp:79-153) for every owed visit, in a fixed
-//           conflict-free order: four passes over 32x32 tiles by tile colour
-//           (tx%2, tz%2); inside a tile, nine cell colours (x%3, z%3) with a
-//           block barrier between them. Cells of one colour, and tiles of one
-//           colour, touch disjoint 3x3 neighbourhoods, so every cascade sees
-//           the latest heights, as in the reference, and the whole step has
-//           one order independent of thread scheduling.
+// One erode cycle (the World::erode(P) call, world.hpp:36-77) is ONE
+// persistent cooperative kernel, k_par_cycle, whose phases are separated by a
+// grid barrier:
+//   spawn     zero the track accumulators, spawn P particles
+//   per step (at most max_age + 2 steps, until no particle is alive):
+//     fly     every live particle runs Wind::fly (wind.hpp:28-117) against
+//             the heights as they were at the start of the step (nothing
+//             writes H in this phase). Its erosion/deposition exchange
+//             (wind.hpp:110-112) is added to the delta map D and the cascade
+//             it owes its cell (wind.hpp:114) to the visit map C, with integer
+//             atomics; survivors are compacted into the other particle buffer.
+//     colour  nine phases, cell colour (x%3, z%3). Colour 0 first adds the
+//             pending exchange deltas (H += D, D = 0) of the 3x3 block around
+//             each colour-0 cell; these blocks tile the map, so that is the
+//             same as adding every delta before the first cascade. Then, in
+//             every colour phase, every cell with C > 0 runs
+//             World::cascade (world.hpp:79-153) up to C times on the current
+//             heights, stopping once a cascade moves nothing (repeating it
+//             could not change anything). Cells of one colour touch disjoint
+//             3x3 neighbourhoods, so no two threads touch the same cell.
+//   ema       tracks -> float, EMA of massflow/momentum (world.hpp:70-76),
+//             fixed-point heights -> float.
 // Every exchange and transfer moves the same integer amount out of one place
 // and into another, so heights + carried + exported sediment is conserved
-// exactly; the result is bitwise reproducible.
+// exactly, and the phase order makes the result bitwise reproducible.
 //
 // Heights are Q(31-f).f fixed point (f = frac_bits); tracks are 64-bit
 // integers in units of 2^-32; particle sediment is fixed point like heights.
-// Survivors of a step are compacted into the other particle buffer with a
-// warp ballot and one atomic per warp.
+//
+// The grid barrier spins with an explicit deadline: a block that waits longer
+// than 2 s sets SWE_STATUS_TIMEOUT and an abort flag, and every block then
+// leaves the kernel at its next barrier, so the kernel always ends.
 #include "swe_device.cuh"
 #include "swe_kernels.h"
 
@@ -37,9 +41,12 @@ namespace {
 constexpr float kTwo32 = 4294967296.0f;
 constexpr float kInvTwo32 = 2.3283064365386963e-10f;
 constexpr float kSqrt2 = 1.41421354f;  // sqrtf(2.0f), correctly rounded
+constexpr int kCycleThreads = 256;
+constexpr int kCycleBlocksPerSm = 4;  // 64 registers per thread, no spills
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
+constexpr unsigned kBarrierLeaves = 16;
 
 __device__ __forceinline__ float fx2f(int32_t q, float inv) { return __int2float_rn(q) * inv; }
-
 __device__ __forceinline__ int32_t wrap_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 __device__ __forceinline__ int32_t wrap_sub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
 
@@ -48,6 +55,84 @@ __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.release.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier of a cooperative launch (all blocks co-resident), as a
+// two-level tree of release/acquire atomics (no separate fences): thread 0
+// of each block arrives on one of kBarrierLeaves leaf counters (separate
+// 128-byte lines, so arrivals do not serialise on one address); the last
+// arrival at a leaf arrives at the root; the last arrival at the root resets
+// it and bumps the generation everyone waits on with acquire loads. The
+// block barriers before and after carry the rest of the block's threads.
+// Returns false if the kernel must stop.
+__device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = ld_acquire(&gb->gen);
+    const unsigned leaf = blockIdx.x % kBarrierLeaves;
+    const unsigned leaf_size = gridDim.x / kBarrierLeaves + (leaf < gridDim.x % kBarrierLeaves ? 1u : 0u);
+    const unsigned nleaves = gridDim.x < kBarrierLeaves ? gridDim.x : kBarrierLeaves;
+    bool last = false;
+    if (atom_add_acq_rel(&gb->leaf[leaf * 32], 1u) == leaf_size - 1) {
+      st_relaxed(&gb->leaf[leaf * 32], 0u);
+      last = atom_add_acq_rel(&gb->count, 1u) == nleaves - 1;
+    }
+    if (last) {
+      st_relaxed(&gb->count, 0u);
+      atom_add_release(&gb->gen, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire(&gb->gen) == g) {
+        if (ld_acquire(&gb->abort)) {
+          ok = 0;
+          break;
+        }
+        if (global_ns() - t0 > kBarrierLimitNs) {
+          atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
+          atomicExch(&gb->abort, 1u);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    if (ld_acquire(&gb->abort)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
 }
 
 __global__ void k_height_to_fixed(const float* __restrict__ H, int32_t* __restrict__ Q, Consts c, Counters* cnt) {
@@ -61,21 +146,38 @@ __global__ void k_height_to_fixed(const float* __restrict__ H, int32_t* __restri
   if (bad) atomicOr(&cnt->status, 0x2u);  // SWE_STATUS_RANGE
 }
 
-__global__ void k_par_spawn(ParallelBuffers B, Consts c, uint32_t seed_lo, uint32_t seed_hi, Counters* cnt,
-                            int particles, long n_cells) {
-  const unsigned long long cyc = cnt->cycle;
-  const uint32_t c_lo = (uint32_t)cyc, c_hi = (uint32_t)(cyc >> 32);
-  const long total = n_cells > particles ? n_cells : particles;
-  const ParticleSoA S = B.state[0];
+struct CycleArgs {
+  ParallelBuffers B;
+  Fields F;
+  Consts c;
+  uint32_t seed_lo, seed_hi;
+  Counters* cnt;
+  GridBarrier* gb;
+  int particles;
+};
+
+// Per-thread tallies of the colour phases.
+struct CascadeStats {
+  unsigned long long transfers = 0;  // transfers that moved a non-zero amount
+  unsigned long long cascades = 0;   // World::cascade evaluations
+  unsigned long long cells = 0;      // cells with owed cascades
+  unsigned int max_iters = 0;        // most cascades one cell ran in one step
+};
+
+// Spawn phase: zero the tracks, spawn particles uniformly in cells with a
+// 1/1000-quantised offset (world.hpp:52-54).
+__device__ void spawn_phase(const CycleArgs& A, uint32_t c_lo, uint32_t c_hi) {
+  const long n = (long)A.c.nx * A.c.nz;
+  const long total = n > A.particles ? n : A.particles;
+  const ParticleSoA S = A.B.state[0];
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    if (i < n_cells) {
-      B.tq[0][i] = 0; B.tq[1][i] = 0; B.tq[2][i] = 0; B.tq[3][i] = 0;
+    if (i < n) {
+      A.B.tq[0][i] = 0; A.B.tq[1][i] = 0; A.B.tq[2][i] = 0; A.B.tq[3][i] = 0;
     }
-    if (i < particles) {
-      // Uniform cell plus a 1/1000-quantised offset, as world.hpp:52-54.
-      const uint4 u = philox4x32((uint32_t)i, 0xFFFFFFFFu, c_lo, c_hi, seed_lo, seed_hi);
-      const int x = (int)(u.x % (uint32_t)c.nx);
-      const int z = (int)(u.y % (uint32_t)c.nz);
+    if (i < A.particles) {
+      const uint4 u = philox4x32((uint32_t)i, 0xFFFFFFFFu, c_lo, c_hi, A.seed_lo, A.seed_hi);
+      const int x = (int)(u.x % (uint32_t)A.c.nx);
+      const int z = (int)(u.y % (uint32_t)A.c.nz);
       const int fxq = (int)(u.z % 1000u);
       const int fzq = (int)(u.w % 1000u);
       S.id[i] = (int)i;
@@ -88,25 +190,20 @@ __global__ void k_par_spawn(ParallelBuffers B, Consts c, uint32_t seed_lo, uint3
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    cnt->live[0] = particles;
-    cnt->live[1] = 0;
-    cnt->particles += (unsigned long long)particles;
+    A.cnt->live[0] = A.particles;
+    A.cnt->live[1] = 0;
+    A.cnt->particles += (unsigned long long)A.particles;
   }
 }
 
-// One Wind::fly step of every live particle against the step-start heights
-// H. The exchange with the cell goes to the delta map D and the visit to the
-// count map C; the cascade runs afterwards in k_par_cascade.
-__global__ void __launch_bounds__(256) k_par_fly(ParallelBuffers B, Consts c, uint32_t seed_lo, uint32_t seed_hi,
-                                                 Counters* cnt, int step) {
+// Fly phase of one step: Wind::fly for every live particle against the
+// step-start heights.
+__device__ void fly_phase(const CycleArgs& A, int step, int count, uint32_t c_lo, uint32_t c_hi) {
+  const Consts& c = A.c;
   const int in = step & 1, outp = in ^ 1;
-  const int count = cnt->live[in];
-  if (count == 0) return;
-  const unsigned long long cyc = cnt->cycle;
-  const uint32_t c_lo = (uint32_t)cyc, c_hi = (uint32_t)(cyc >> 32);
-  const ParticleSoA S = B.state[in];
-  const ParticleSoA Dst = B.state[outp];
-  const int32_t* __restrict__ H = B.hq;
+  const ParticleSoA S = A.B.state[in];
+  const ParticleSoA Dst = A.B.state[outp];
+  const int32_t* H = A.B.hq;
   const int nx = c.nx, nz = c.nz;
   const float inv = c.inv_scale;
 
@@ -134,11 +231,11 @@ __global__ void __launch_bounds__(256) k_par_fly(ParallelBuffers B, Consts c, ui
       if (!dies) {
         const bool vx0 = ix > 0, vx2 = ix + 1 < nx, vz0 = iz > 0, vz2 = iz + 1 < nz;
         const long ci = (long)ix * nz + iz;
-        const float h11 = fx2f(__ldg(H + ci), inv);
-        const float h01 = vx0 ? fx2f(__ldg(H + ci - nz), inv) : 0.0f;
-        const float h21 = vx2 ? fx2f(__ldg(H + ci + nz), inv) : 0.0f;
-        const float h10 = vz0 ? fx2f(__ldg(H + ci - 1), inv) : 0.0f;
-        const float h12 = vz2 ? fx2f(__ldg(H + ci + 1), inv) : 0.0f;
+        const float h11 = fx2f(H[ci], inv);
+        const float h01 = vx0 ? fx2f(H[ci - nz], inv) : 0.0f;
+        const float h21 = vx2 ? fx2f(H[ci + nz], inv) : 0.0f;
+        const float h10 = vz0 ? fx2f(H[ci - 1], inv) : 0.0f;
+        const float h12 = vz2 ? fx2f(H[ci + 1], inv) : 0.0f;
 
         // quad::_normal (cellpool.h:200-223) on the step-start heights.
         V3 n = v3(0.0f, 0.0f, 0.0f);
@@ -165,7 +262,7 @@ __global__ void __launch_bounds__(256) k_par_fly(ParallelBuffers B, Consts c, ui
           if (collision < 0.0f) collision = 0.0f;
           const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
           sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
-          const uint4 u = philox4x32((uint32_t)id, (uint32_t)step, c_lo, c_hi, seed_lo, seed_hi);
+          const uint4 u = philox4x32((uint32_t)id, (uint32_t)step, c_lo, c_hi, A.seed_lo, A.seed_hi);
           const float rx = (float)(int)(u.x % 1001u), ry = (float)(int)(u.y % 1001u), rz = (float)(int)(u.z % 1001u);
           sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
           const float drag = 1.0f - 0.3f * sed;
@@ -182,15 +279,15 @@ __global__ void __launch_bounds__(256) k_par_fly(ParallelBuffers B, Consts c, ui
             dies = true;
           } else {
             // Tracks of the pre-move cell (wind.hpp:93-96).
-            atomicAdd((unsigned long long*)&B.tq[0][ci], (unsigned long long)to_fixed64(sed * kTwo32));
-            atomicAdd((unsigned long long*)&B.tq[1][ci], (unsigned long long)to_fixed64(sp.x * kTwo32));
-            atomicAdd((unsigned long long*)&B.tq[2][ci], (unsigned long long)to_fixed64(sp.y * kTwo32));
-            atomicAdd((unsigned long long*)&B.tq[3][ci], (unsigned long long)to_fixed64(sp.z * kTwo32));
+            atomicAdd((unsigned long long*)&A.B.tq[0][ci], (unsigned long long)to_fixed64(sed * kTwo32));
+            atomicAdd((unsigned long long*)&A.B.tq[1][ci], (unsigned long long)to_fixed64(sp.x * kTwo32));
+            atomicAdd((unsigned long long*)&A.B.tq[2][ci], (unsigned long long)to_fixed64(sp.y * kTwo32));
+            atomicAdd((unsigned long long*)&A.B.tq[3][ci], (unsigned long long)to_fixed64(sp.z * kTwo32));
             // Exchange with the cell (wind.hpp:110-112), in fixed point, and
             // one cascade owed to the cell (wind.hpp:114).
             const int32_t ex_q = to_fixed(c.suspension * diff * c.scale);
-            atomicAdd(B.dq + ci, -ex_q);
-            atomicAdd(B.visits + ci, 1);
+            atomicAdd(A.B.dq + ci, -ex_q);
+            atomicAdd(A.B.visits + ci, 1);
             sed_q = wrap_add(sed_q, ex_q);
             px = npx; py = npy; pz = npz;
             vx = sp.x; vy = sp.y; vz = sp.z;
@@ -204,7 +301,7 @@ __global__ void __launch_bounds__(256) k_par_fly(ParallelBuffers B, Consts c, ui
     // Compact survivors into the other buffer: one atomic per warp.
     const unsigned mask = __ballot_sync(0xffffffffu, alive);
     int slot0 = 0;
-    if (lane == 0 && mask) slot0 = atomicAdd(&cnt->live[outp], __popc(mask));
+    if (lane == 0 && mask) slot0 = atomicAdd(&A.cnt->live[outp], __popc(mask));
     slot0 = __shfl_sync(0xffffffffu, slot0, 0);
     if (alive) {
       const int o = slot0 + __popc(mask & ((1u << lane) - 1u));
@@ -217,166 +314,398 @@ __global__ void __launch_bounds__(256) k_par_fly(ParallelBuffers B, Consts c, ui
   steps = warp_sum(steps);
   status = __reduce_or_sync(0xffffffffu, status);
   if (lane == 0) {
-    if (exported) atomicAdd((unsigned long long*)&cnt->exported_q, (unsigned long long)exported);
-    if (steps) atomicAdd(&cnt->particle_steps, steps);
-    if (status) atomicOr(&cnt->status, status);
+    if (exported) atomicAdd((unsigned long long*)&A.cnt->exported_q, (unsigned long long)exported);
+    if (steps) atomicAdd(&A.cnt->particle_steps, steps);
+    if (status) atomicOr(&A.cnt->status, status);
   }
 }
 
-constexpr int kTile = 32;          // cells per tile side
-constexpr int kLs = kTile + 2;     // with the one-cell halo
-constexpr int kCascadeThreads = 128;
+// Thresholds of one cascade, in both forms used below.
+struct CascadeConsts {
+  float md1, md2;  // slope limit d*maxdiff of axis / diagonal neighbours
+  float hd1, hd2;  // the same in half fixed-point steps (exact power-of-two scaling)
+  bool unit;       // settling == 1
+};
 
-// World::cascade (world.hpp:79-153) in fixed point on the shared-memory
-// tile: neighbours in the reference's order, stable descending by their
-// current height (original order breaks ties), each moving half the excess
-// over the slope limit. Ranks instead of a sort keep everything in
-// registers.
-__device__ __forceinline__ int cascade_smem(int32_t (*L)[kLs], int li, int lj, bool vx0, bool vx2, bool vz0,
-                                            bool vz2, const Consts& c) {
-  const bool val[8] = {vx0 && vz0, vx0, vx0 && vz2, vz0, vz2, vx2 && vz0, vx2, vx2 && vz2};
-  int32_t key[8];
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    const int a = k < 3 ? 0 : (k < 5 ? 1 : 2);
-    const int b = (k == 0 || k == 3 || k == 5) ? 0 : ((k == 1 || k == 6) ? 1 : 2);
-    key[k] = L[li + a - 1][lj + b - 1];
+// Whether a transfer from/to a neighbour at fixed-point height difference dq
+// moves a non-zero amount, and how much (World::cascade, world.hpp:132-143:
+// transfer = settling * (|diff| - d*maxdiff) / 2). With settling == 1 and
+// |dq| < 2^24 the amount rint(((|dq| 2^-f - dmax) * 0.5) * 2^f) equals
+// rint(0.5 |dq| - dmax 2^(f-1)) exactly (scaling by powers of two commutes
+// with rounding and |dq| is exact in float), and it is non-zero exactly when
+// 0.5 |dq| - dmax 2^(f-1) > 0.5.
+__device__ __forceinline__ int32_t transfer_q(int32_t dq, bool axis, const CascadeConsts& k, const Consts& c) {
+  const int32_t adq = dq < 0 ? -dq : dq;
+  if (adq == 0) return 0;
+  if (k.unit && adq < (1 << 24)) {
+    const float u = fmaf(0.5f, __int2float_rn(adq), axis ? -k.hd1 : -k.hd2);
+    return u > 0.5f ? __float2int_rn(u) : 0;
   }
-  int rank[8];
-  int num = 0;
+  const float excess = fabsf(__int2float_rn(dq) * c.inv_scale) - (axis ? k.md1 : k.md2);
+  if (excess <= 0.0f) return 0;
+  return to_fixed(c.settling * excess * 0.5f * c.scale);
+}
+
+// World::cascade (world.hpp:79-153) in fixed point on the 3x3 neighbourhood
+// N (shared memory, N[3*u+v] is cell (x+u-1, z+v-1)). The in-bounds
+// neighbours are ordered by height, largest first, equal heights in the
+// reference's neighbour order (std::sort on <= 16 elements is a stable
+// insertion sort): the sort keys pack 8*height + (7 - neighbour index) into
+// Key (int32 when all nine heights are below 2^27 in magnitude, else int64)
+// and go through Knuth's optimal 19-comparator network. The transfers then
+// run against the running centre height. A cascade that moves nothing leaves
+// the centre unchanged, so a first pass decides that case against the
+// current centre in any order and skips the sort. Returns the number of
+// transfers that moved a non-zero amount. This general form serves any
+// settling and any height range.
+template <class Key>
+__device__ __forceinline__ int cascade_general(int32_t* N, const bool (&val)[8], const CascadeConsts& kc,
+                                               const Consts& c) {
+  constexpr int slot[8] = {0, 1, 2, 3, 5, 6, 7, 8};
+  constexpr unsigned kAxisMask = 0x5Au;  // neighbours 1, 3, 4, 6 are axis-aligned
+  const int32_t h0 = N[4];
+  bool any = false;
 #pragma unroll
-  for (int k = 0; k < 8; k++) {
-    num += val[k] ? 1 : 0;
-    int r = 0;
+  for (int k = 0; k < 8; k++)
+    any |= val[k] && transfer_q(wrap_sub(h0, N[slot[k]]), (kAxisMask >> k) & 1u, kc, c) != 0;
+  if (!any) return 0;
+
+  const Key kNone = (Key)1 << (sizeof(Key) * 8 - 1);  // most negative: sorts last
+  Key v[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      if (j == k) continue;
-      r += (val[j] && (key[j] > key[k] || (j < k && key[j] == key[k]))) ? 1 : 0;
-    }
-    rank[k] = val[k] ? r : 8;
+  for (int k = 0; k < 8; k++) v[k] = val[k] ? (Key)N[slot[k]] * 8 + (Key)(7 - k) : kNone;
+#define SWE_CE(a, b)                                  \
+  {                                                   \
+    const Key hi = v[a] > v[b] ? v[a] : v[b];         \
+    const Key lo = v[a] > v[b] ? v[b] : v[a];         \
+    v[a] = hi;                                        \
+    v[b] = lo;                                        \
   }
-  int32_t hc = L[li][lj];
-  int32_t dl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  SWE_CE(0, 1) SWE_CE(2, 3) SWE_CE(4, 5) SWE_CE(6, 7)
+  SWE_CE(0, 2) SWE_CE(1, 3) SWE_CE(4, 6) SWE_CE(5, 7)
+  SWE_CE(1, 2) SWE_CE(5, 6) SWE_CE(0, 4) SWE_CE(3, 7)
+  SWE_CE(1, 5) SWE_CE(2, 6)
+  SWE_CE(1, 4) SWE_CE(3, 6)
+  SWE_CE(2, 4) SWE_CE(3, 5)
+  SWE_CE(3, 4)
+  int32_t hc = h0;
   int transfers = 0;
-  for (int r = 0; r < num; r++) {
-    int32_t kq = 0;
-    float d = 1.0f;
-    int sel = 0;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      if (rank[k] == r) {
-        kq = key[k];
-        d = (k == 1 || k == 3 || k == 4 || k == 6) ? 1.0f : kSqrt2;
-        sel = k;
-      }
-    }
-    const long long dq = (long long)hc - (long long)kq;
-    if (dq == 0) continue;
-    const float excess = fabsf(__ll2float_rn(dq) * c.inv_scale) - d * c.maxdiff;
-    if (excess <= 0.0f) continue;
-    const int32_t tq = to_fixed(c.settling * excess / 2.0f * c.scale);
-    const int32_t sgn = dq > 0 ? tq : -tq;
+  for (int r = 0; r < 8; r++) {
+    if (v[r] == kNone) break;
+    const int k = 7 - (int)(v[r] & 7);
+    const int32_t tq = transfer_q(wrap_sub(hc, (int32_t)(v[r] >> 3)), (kAxisMask >> k) & 1u, kc, c);
+    if (tq == 0) continue;
+    const int32_t sgn = wrap_sub(hc, (int32_t)(v[r] >> 3)) > 0 ? tq : -tq;
     hc = wrap_sub(hc, sgn);
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-      if (k == sel) dl[k] = wrap_add(dl[k], sgn);
+    const int sl = k < 4 ? k : k + 1;
+    N[sl] = wrap_add(N[sl], sgn);
     transfers++;
   }
-  L[li][lj] = hc;
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    if (dl[k] != 0) {
-      const int a = k < 3 ? 0 : (k < 5 ? 1 : 2);
-      const int b = (k == 0 || k == 3 || k == 5) ? 0 : ((k == 1 || k == 6) ? 1 : 2);
-      L[li + a - 1][lj + b - 1] = wrap_add(L[li + a - 1][lj + b - 1], dl[k]);
-    }
-  }
+  N[4] = hc;
   return transfers;
 }
 
-// One cascade pass over the tiles of colour (color>>1, color&1). A block
-// loads its 32x32 tile plus halo (heights + pending exchange deltas), runs
-// every owed cascade colour by colour (x%3, z%3) with a block barrier
-// between colours, and writes the tile back: own cells absorb their deltas,
-// halo cells go back without theirs (their own tile absorbs them).
-__global__ void __launch_bounds__(kCascadeThreads) k_par_cascade(ParallelBuffers B, Consts c, Counters* cnt,
-                                                                 int step, int color, int tiles_z) {
-  const int surv = cnt->live[(step + 1) & 1];
-  if (color == 0 && blockIdx.x == 0 && threadIdx.x == 0) cnt->live[step & 1] = 0;
-  if (surv == 0) return;
-  __shared__ int32_t L[kLs][kLs];
-  const int nx = c.nx, nz = c.nz;
-  const int tx = (color >> 1) + 2 * (blockIdx.x / tiles_z);
-  const int tz = (color & 1) + 2 * (blockIdx.x % tiles_z);
-  const int x0 = tx * kTile, z0 = tz * kTile;
-  int32_t* __restrict__ H = B.hq;
-  int32_t* __restrict__ Dq = B.dq;
-  int32_t* __restrict__ V = B.visits;
-
-  for (int idx = threadIdx.x; idx < kLs * kLs; idx += kCascadeThreads) {
-    const int i = idx / kLs, j = idx % kLs;
-    const int x = x0 + i - 1, z = z0 + j - 1;
-    int32_t v = 0;
-    if (x >= 0 && z >= 0 && x < nx && z < nz) {
-      const long g = (long)x * nz + z;
-      v = wrap_add(H[g], Dq[g]);
-    }
-    L[i][j] = v;
+// The same cascade for the common case, settling == 1 and all nine heights
+// within 2^24 fixed-point steps of each other: the centre then stays within
+// that range, every |dq| < 2^24, and each transfer is
+// rint(0.5 |dq| - dmax 2^(f-1)) when that exceeds 0.5 (see transfer_q).
+// Branch-free: the whole chain is selects in registers, and each neighbour's
+// new height (its sort key's height plus its transfer) is stored after the
+// chain.
+__device__ __forceinline__ int cascade_unit(int32_t* N, const bool (&val)[8], float hd1, float hd2) {
+  constexpr int slot[8] = {0, 1, 2, 3, 5, 6, 7, 8};
+  constexpr unsigned kAxisMask = 0x5Au;
+  const int32_t kNone = (int32_t)0x80000000u;
+  int32_t h[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) h[k] = N[slot[k]];
+  const int32_t h0 = N[4];
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int32_t d = h0 - h[k];
+    const int32_t ad = d < 0 ? -d : d;
+    const float u = fmaf(0.5f, __int2float_rn(ad), ((kAxisMask >> k) & 1u) ? -hd1 : -hd2);
+    any |= val[k] && ad != 0 && u > 0.5f;
   }
-  __syncthreads();
-
+  if (!any) return 0;
+  int32_t v[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = val[k] ? h[k] * 8 + (7 - k) : kNone;
+#define SWE_CE(a, b)                       \
+  {                                        \
+    const int32_t hi = max(v[a], v[b]);    \
+    const int32_t lo = min(v[a], v[b]);    \
+    v[a] = hi;                             \
+    v[b] = lo;                             \
+  }
+  SWE_CE(0, 1) SWE_CE(2, 3) SWE_CE(4, 5) SWE_CE(6, 7)
+  SWE_CE(0, 2) SWE_CE(1, 3) SWE_CE(4, 6) SWE_CE(5, 7)
+  SWE_CE(1, 2) SWE_CE(5, 6) SWE_CE(0, 4) SWE_CE(3, 7)
+  SWE_CE(1, 5) SWE_CE(2, 6)
+  SWE_CE(1, 4) SWE_CE(3, 6)
+  SWE_CE(2, 4) SWE_CE(3, 5)
+  SWE_CE(3, 4)
+#undef SWE_CE
+  int32_t hc = h0;
+  int32_t sg[8];
   int transfers = 0;
-  const int t = threadIdx.x;
-  const int m = t / 11, l = t % 11;
-#pragma unroll 1
-  for (int col = 0; col < 9; col++) {
-    const int a = col / 3, b = col % 3;
-    const int i = ((a - x0 % 3) + 3) % 3 + 3 * m;
-    const int j = ((b - z0 % 3) + 3) % 3 + 3 * l;
-    const int x = x0 + i, z = z0 + j;
-    if (t < 121 && i < kTile && j < kTile && x < nx && z < nz) {
-      const int visits = V[(long)x * nz + z];
-      for (int r = 0; r < visits; r++)
-        transfers += cascade_smem(L, i + 1, j + 1, x > 0, x + 1 < nx, z > 0, z + 1 < nz, c);
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const bool ok = v[r] != kNone;
+    const int k = 7 - (v[r] & 7);
+    const int32_t kq = v[r] >> 3;
+    const int32_t dq = wrap_sub(hc, kq);  // sentinel entries are masked by `ok`
+    const int32_t ad = dq < 0 ? wrap_sub(0, dq) : dq;
+    const float u = fmaf(0.5f, __int2float_rn(ad), ((kAxisMask >> k) & 1u) ? -hd1 : -hd2);
+    const bool move = ok && ad != 0 && u > 0.5f;
+    const int32_t tq = move ? __float2int_rn(u) : 0;
+    sg[r] = dq > 0 ? tq : -tq;
+    hc = wrap_sub(hc, sg[r]);
+    transfers += move ? 1 : 0;
+  }
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    if (v[r] != kNone) {
+      const int k = 7 - (v[r] & 7);
+      N[k < 4 ? k : k + 1] = (v[r] >> 3) + sg[r];
+    }
+  }
+  N[4] = hc;
+  return transfers;
+}
+
+// Colour phase: the owed cascades of every cell of colour (a, b).
+//
+// The 3x3 blocks around the colour-(0,0) cells tile the map (with virtual
+// centres one step past the far edges), so the colour-0 phase first adds
+// every cell's pending exchange delta, block by block: the same as adding
+// all deltas before the first cascade.
+//
+// Each thread takes one cell and loads its 3x3 neighbourhood into its slice
+// of shared memory; the cells that owe cascades are then compacted into a
+// block-local list, and the block's threads work through that list densely,
+// so warps are not held up by the threads whose cells owe nothing.
+__device__ void colour_phase(const CycleArgs& A, int a, int b, int32_t* nb, int* list, int* owed, int* wcount,
+                             CascadeStats& st) {
+  const Consts& c = A.c;
+  const int nx = c.nx, nz = c.nz;
+  const bool absorb = (a == 0 && b == 0);
+  const int cx = absorb ? nx / 3 + 1 : (nx - a + 2) / 3;
+  const int cz = absorb ? nz / 3 + 1 : (nz - b + 2) / 3;
+  const int cells = cx * cz;
+  int32_t* H = A.B.hq;
+  int32_t* Dq = A.B.dq;
+  int32_t* V = A.B.visits;
+  CascadeConsts kc;
+  kc.md1 = 1.0f * c.maxdiff;
+  kc.md2 = kSqrt2 * c.maxdiff;
+  kc.hd1 = kc.md1 * (0.5f * c.scale);
+  kc.hd2 = kc.md2 * (0.5f * c.scale);
+  kc.unit = c.settling == 1.0f;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int32_t* N = nb + 9 * t;
+  for (int base = blockIdx.x * blockDim.x; base < cells; base += gridDim.x * blockDim.x) {
+    const int i = base + t;
+    int visits = 0;
+    if (i < cells) {
+      const int ix = i / cz;
+      const int x = a + 3 * ix, z = b + 3 * (i - ix * cz);
+      const long g = (long)x * nz + z;
+      if (x < nx && z < nz) {
+        visits = V[g];
+        if (visits) V[g] = 0;
+      }
+      if (absorb || visits) {
+        bool changed = false;
+#pragma unroll
+        for (int u = 0; u < 3; u++) {
+#pragma unroll
+          for (int w = 0; w < 3; w++) {
+            const bool ok = (u == 0 ? x > 0 : (u == 2 ? x + 1 < nx : x < nx)) &&
+                            (w == 0 ? z > 0 : (w == 2 ? z + 1 < nz : z < nz));
+            int32_t h = 0;
+            if (ok) {
+              const long q = g + (long)(u - 1) * nz + (w - 1);
+              h = H[q];
+              if (absorb) {
+                const int32_t d = Dq[q];
+                if (d != 0) {
+                  h = wrap_add(h, d);
+                  Dq[q] = 0;
+                  changed = true;
+                }
+              }
+            }
+            N[3 * u + w] = h;
+          }
+        }
+        if (changed && !visits) {
+#pragma unroll
+          for (int u = 0; u < 3; u++) {
+#pragma unroll
+            for (int w = 0; w < 3; w++) {
+              const bool ok = (u == 0 ? x > 0 : (u == 2 ? x + 1 < nx : x < nx)) &&
+                              (w == 0 ? z > 0 : (w == 2 ? z + 1 < nz : z < nz));
+              if (ok) H[g + (long)(u - 1) * nz + (w - 1)] = N[3 * u + w];
+            }
+          }
+        }
+      }
+    }
+    // Compact the threads whose cell owes cascades.
+    const unsigned m = __ballot_sync(0xffffffffu, visits != 0);
+    if (lane == 0) wcount[warp] = __popc(m);
+    owed[t] = visits;
+    __syncthreads();
+    int off = 0, total = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      const int n = wcount[k];
+      off += k < warp ? n : 0;
+      total += n;
+    }
+    if (visits) list[off + __popc(m & ((1u << lane) - 1u))] = t;
+    __syncthreads();
+    if (t < total) {
+      const int o = list[t];
+      const int io = base + o;
+      const int ix = io / cz;
+      const int x = a + 3 * ix, z = b + 3 * (io - ix * cz);
+      const long g = (long)x * nz + z;
+      int32_t* M = nb + 9 * o;
+      const int vis = owed[o];
+      const bool vx0 = x > 0, vx2 = x + 1 < nx, vz0 = z > 0, vz2 = z + 1 < nz;
+      const bool val[8] = {vx0 && vz0, vx0, vx0 && vz2, vz0, vz2, vx2 && vz0, vx2, vx2 && vz2};
+      // The common case takes the branch-free cascade: settling == 1 and the
+      // nine heights (of in-bounds cells) within 2^24 steps of each other;
+      // cascades keep every height inside the initial range.
+      int32_t lo = M[4], hi = M[4];
+      bool big = false;
+#pragma unroll
+      for (int s9 = 0; s9 < 9; s9++) {
+        const bool in = (s9 == 4) || val[s9 < 4 ? s9 : s9 - 1];
+        const int32_t h = M[s9];
+        if (in) {
+          lo = min(lo, h);
+          hi = max(hi, h);
+          big |= (h < 0 ? -h : h) >= (1 << 27);
+        }
+      }
+      const bool unit = kc.unit && !big && (long long)hi - (long long)lo < (1ll << 24);
+      int it = 0;
+      for (int r = 0; r < vis; r++) {
+        const int tr = unit ? cascade_unit(M, val, kc.hd1, kc.hd2)
+                            : (big ? cascade_general<long long>(M, val, kc, c) : cascade_general<int32_t>(M, val, kc, c));
+        it++;
+        if (tr == 0) break;
+        st.transfers += (unsigned long long)tr;
+      }
+      st.cascades += (unsigned long long)it;
+      st.cells += 1;
+      if ((unsigned)it > st.max_iters) st.max_iters = (unsigned)it;
+#pragma unroll
+      for (int u = 0; u < 3; u++) {
+#pragma unroll
+        for (int w = 0; w < 3; w++) {
+          const bool ok = (u == 0 ? vx0 : (u == 2 ? vx2 : true)) && (w == 0 ? vz0 : (w == 2 ? vz2 : true));
+          if (ok) H[g + (long)(u - 1) * nz + (w - 1)] = M[3 * u + w];
+        }
+      }
     }
     __syncthreads();
   }
-
-  for (int idx = threadIdx.x; idx < kLs * kLs; idx += kCascadeThreads) {
-    const int i = idx / kLs, j = idx % kLs;
-    const int x = x0 + i - 1, z = z0 + j - 1;
-    if (x < 0 || z < 0 || x >= nx || z >= nz) continue;
-    const long g = (long)x * nz + z;
-    const bool own = i >= 1 && j >= 1 && i <= kTile && j <= kTile;
-    if (own) {
-      H[g] = L[i][j];
-      Dq[g] = 0;
-      V[g] = 0;
-    } else {
-      H[g] = wrap_sub(L[i][j], Dq[g]);
-    }
-  }
-  const int tw = warp_sum(transfers);
-  if ((threadIdx.x & 31) == 0 && tw) atomicAdd(&cnt->transfers, (unsigned long long)tw);
 }
 
-// Tracks to float, EMA (world.hpp:70-76), heights to float; count the cycle.
-__global__ void k_par_ema(ParallelBuffers B, Fields F, Consts c, Counters* cnt, long n) {
+// Tracks to float, EMA (world.hpp:70-76), heights to float.
+__device__ void ema_phase(const CycleArgs& A) {
+  const long n = (long)A.c.nx * A.c.nz;
   unsigned bad = 0;
-  const float lrate = c.lrate;
+  const float lrate = A.c.lrate;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const float t = __ll2float_rn(B.tq[k][i]) * kInvTwo32;
-      F.f[5 + k][i] = t;
-      F.f[1 + k][i] = (1.0f - lrate) * F.f[1 + k][i] + lrate * t;
+      const float t = __ll2float_rn(A.B.tq[k][i]) * kInvTwo32;
+      A.F.f[5 + k][i] = t;
+      A.F.f[1 + k][i] = (1.0f - lrate) * A.F.f[1 + k][i] + lrate * t;
     }
-    const int32_t q = B.hq[i];
+    const int32_t q = A.B.hq[i];
     if (q > 1073741823 || q < -1073741823) bad = 1;
-    F.f[0][i] = fx2f(q, c.inv_scale);
+    A.F.f[0][i] = fx2f(q, A.c.inv_scale);
   }
-  if (bad) atomicOr(&cnt->status, 0x2u);
-  if (blockIdx.x == 0 && threadIdx.x == 0) cnt->cycle += 1;
+  if (bad) atomicOr(&A.cnt->status, 0x2u);
+}
+
+__global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(CycleArgs A) {
+  // Per-thread 3x3 neighbourhood of the colour phases (stride 9 words: the
+  // 32 threads of a warp fall in distinct banks).
+  __shared__ int32_t nb[kCycleThreads * 9];
+  __shared__ int list[kCycleThreads];
+  __shared__ int owed[kCycleThreads];
+  __shared__ int wcount[kCycleThreads / 32];
+  Counters* cnt = A.cnt;
+  const unsigned long long cyc = cnt->cycle;
+  const uint32_t c_lo = (uint32_t)cyc, c_hi = (uint32_t)(cyc >> 32);
+  // Block 0's thread 0 times the phases (each including its closing barrier).
+  const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long tph[13] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long t_mark = timer ? global_ns() : 0;
+  auto lap = [&](int k) {
+    if (timer) {
+      const unsigned long long t = global_ns();
+      tph[k] += t - t_mark;
+      t_mark = t;
+    }
+  };
+
+  spawn_phase(A, c_lo, c_hi);
+  if (!grid_sync(A.gb, &cnt->status)) return;
+  lap(0);
+
+  CascadeStats cst;
+  const int nsteps = A.c.max_age + 2;
+  for (int step = 0; step < nsteps; step++) {
+    const int count = ld_volatile(&cnt->live[step & 1]);
+    if (count == 0) break;
+    fly_phase(A, step, count, c_lo, c_hi);
+    if (!grid_sync(A.gb, &cnt->status)) return;
+    lap(1);
+    // Only survivors wrote D and C; with none, the map is already final.
+    const int survivors = ld_volatile(&cnt->live[(step + 1) & 1]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt->live[step & 1] = 0;
+    if (survivors == 0) continue;
+    for (int col = 0; col < 9; col++) {
+      colour_phase(A, col / 3, col % 3, nb, list, owed, wcount, cst);
+      if (!grid_sync(A.gb, &cnt->status)) return;
+      lap(3 + col);
+    }
+  }
+  {
+    const unsigned long long tr = warp_sum(cst.transfers), ca = warp_sum(cst.cascades), ce = warp_sum(cst.cells);
+    unsigned mi = cst.max_iters;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned other = __shfl_xor_sync(0xffffffffu, mi, o);
+      mi = other > mi ? other : mi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (tr) atomicAdd(&cnt->transfers, tr);
+      if (ca) atomicAdd(&cnt->cascades, ca);
+      if (ce) atomicAdd(&cnt->cascade_cells, ce);
+      if (mi) atomicMax(&cnt->max_cascade_iters, mi);
+    }
+  }
+
+  ema_phase(A);
+  lap(12);
+  if (timer) {
+    cnt->cycle = cyc + 1;
+    cnt->fly_ns += tph[1];
+    unsigned long long cas = 0;
+    for (int k = 3; k < 12; k++) cas += tph[k];
+    cnt->cascade_ns += cas;
+    for (int k = 0; k < 13; k++) cnt->phase_ns[k] += tph[k];
+  }
 }
 
 __global__ void k_sum_fixed(const int32_t* __restrict__ hq, long n, long long* out) {
@@ -398,48 +727,33 @@ void launch_height_to_fixed(const float* height, int32_t* q, const Consts& c, Co
   k_height_to_fixed<<<sweep_grid((long)c.nx * c.nz), 256, 0, s>>>(height, q, c, cnt);
 }
 
-void launch_par_spawn(const ParallelBuffers& B, const Consts& c, uint64_t seed, Counters* cnt, int particles,
-                      long n_cells, cudaStream_t s) {
-  const long total = n_cells > particles ? n_cells : particles;
-  k_par_spawn<<<sweep_grid(total), 256, 0, s>>>(B, c, (uint32_t)seed, (uint32_t)(seed >> 32), cnt, particles,
-                                                n_cells);
+int cycle_grid(int device) {
+  int sms = 0, per_sm = 0, coop = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_par_cycle, kCycleThreads, 0) != cudaSuccess)
+    return 0;
+  return sms * per_sm;
 }
 
-void launch_par_fly(const ParallelBuffers& B, const Consts& c, uint64_t seed, Counters* cnt, int step, int grid,
-                    cudaStream_t s) {
-  k_par_fly<<<grid, 256, 0, s>>>(B, c, (uint32_t)seed, (uint32_t)(seed >> 32), cnt, step);
-}
-
-void launch_par_cascade(const ParallelBuffers& B, const Consts& c, Counters* cnt, int step, cudaStream_t s) {
-  const int tiles_x = (c.nx + kTile - 1) / kTile, tiles_z = (c.nz + kTile - 1) / kTile;
-  for (int color = 0; color < 4; color++) {
-    const int cx = color >> 1, cz = color & 1;
-    const int gx = (tiles_x - cx + 1) / 2, gz = (tiles_z - cz + 1) / 2;
-    if (gx <= 0 || gz <= 0) {
-      // No tile of this colour; pass 0 still resets the live counter.
-      if (color == 0) k_par_cascade<<<1, kCascadeThreads, 0, s>>>(B, c, cnt, step, color, 1);
-      continue;
-    }
-    k_par_cascade<<<gx * gz, kCascadeThreads, 0, s>>>(B, c, cnt, step, color, gz);
-  }
-}
-
-void launch_par_ema(const ParallelBuffers& B, const Fields& F, const Consts& c, Counters* cnt, long n_cells,
-                    cudaStream_t s) {
-  k_par_ema<<<sweep_grid(n_cells), 256, 0, s>>>(B, F, c, cnt, n_cells);
+cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
+                             Counters* cnt, GridBarrier* gb, int particles, int grid, cudaStream_t s) {
+  CycleArgs A;
+  A.B = B;
+  A.F = F;
+  A.c = c;
+  A.seed_lo = (uint32_t)seed;
+  A.seed_hi = (uint32_t)(seed >> 32);
+  A.cnt = cnt;
+  A.gb = gb;
+  A.particles = particles;
+  void* args[] = {&A};
+  return cudaLaunchCooperativeKernel((const void*)k_par_cycle, dim3(grid), dim3(kCycleThreads), args, 0, s);
 }
 
 void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s) {
   k_sum_fixed<<<sweep_grid(n), 256, 0, s>>>(hq, n, out);
-}
-
-int par_step_grid(int device) {
-  int sms = 0, per_sm = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_par_fly, 256, 0);
-  if (per_sm < 1) per_sm = 1;
-  if (sms < 1) sms = 1;
-  return sms * per_sm;
 }
 
 }  // namespace swe

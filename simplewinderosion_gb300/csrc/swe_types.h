@@ -41,6 +41,24 @@ struct Counters {
   unsigned int pad;
   long long tape_pos;        // ordered mode tape cursor
   unsigned long long cycle;  // parallel mode: cycles completed (RNG counter)
+  unsigned long long fly_ns;      // parallel mode: time in fly phases (block 0's clock)
+  unsigned long long cascade_ns;  // parallel mode: time in apply + colour phases
+  // parallel mode, per phase (block 0's clock, barrier included):
+  // spawn, fly, (unused), colour 0..8, ema
+  unsigned long long phase_ns[13];
+  unsigned long long cascades;       // parallel mode: World::cascade evaluations
+  unsigned long long cascade_cells;  // parallel mode: cell-steps with owed cascades
+  unsigned int max_cascade_iters;    // parallel mode: most cascades of one cell in one step
+  unsigned int pad2;
+};
+
+// State of the grid-wide barrier of the persistent parallel kernel.
+struct GridBarrier {
+  unsigned int count;  // leaf arrivals at the root in the current generation
+  unsigned int gen;    // generation the waiting blocks watch
+  unsigned int abort;  // set by a block that gave up waiting
+  unsigned int pad[29];
+  unsigned int leaf[16 * 32];  // block arrivals per leaf, one 128-byte line each
 };
 
 // Particle state of the parallel mode, structure of arrays.
