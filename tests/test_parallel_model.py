@@ -36,7 +36,7 @@ def _world(n, seed, wind=WIND_101, frac_bits=24, **kw):
     return p, h
 
 
-@pytest.mark.parametrize("n,particles,frac_bits", [(16, 64, 24), (48, 500, 24), (64, 1024, 16), (40, 300, 28)])
+@pytest.mark.parametrize("n,particles,frac_bits", [(16, 64, 24), (48, 500, 24), (64, 1024, 16), (40, 300, 28), (32, 1024, 24), (48, 2304, 16)])
 def test_parallel_model_conserves_mass_exactly(n, particles, frac_bits):
     p, _ = _world(n, 3, frac_bits=frac_bits)
     m0, e0 = p.par_ledger()
