@@ -194,6 +194,32 @@ int swe_world_cascade_stats(swe_world* w, int64_t* cascades, int64_t* cells, int
  * first_bits, first_bits+1, ...; for checking it against the C library. */
 int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host_y);
 
+/* Parallel erosion that allocates no device memory. No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc, such as a
+ * frame loop inside a render or game engine that owns the GPU's memory pool
+ * (the reference's own app erodes once per rendered frame), or code running
+ * while another framework's allocator owns the device memory.
+ *
+ * `fields` are the caller's nine device arrays of nx*nz floats in swe_field
+ * order (inputs and outputs, as a world's fields). The call runs `cycles`
+ * parallel erode cycles of `particles_per_cycle` particles (same results as a
+ * world whose random-number cycle counter is `first_cycle`), enqueued on
+ * `stream` (NULL: the default stream). The scratch it needs lives in one
+ * static device array, about 15.5 MB on every GPU that loads the library,
+ * held until the process exits; its limits are SWE_NOALLOC_MAX_CELLS cells
+ * and SWE_NOALLOC_MAX_PARTICLES particles per cycle, and larger requests fail
+ * with SWE_ERR_INVALID. The first call on a device looks up that array's
+ * device address (set-up, once per device): make that first call before any
+ * stream capture. All calls share the array, so calls that overlap on the GPU
+ * race; serialise them (one stream, or synchronise between them). If
+ * `status` is non-NULL the call waits for the stream and reports the device
+ * status bits (SWE_ERR_DEVICE if any are set). */
+#define SWE_NOALLOC_MAX_CELLS 262144
+#define SWE_NOALLOC_MAX_PARTICLES 65536
+int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, const swe_params* p, uint64_t seed,
+                               uint64_t first_cycle, int cycles, int particles_per_cycle, void* stream,
+                               uint32_t* status);
+
 /* Message of the calling thread's last error ("" if none). */
 const char* swe_last_error(void);
 

@@ -78,6 +78,8 @@ bool params_ok(const swe_params& p, std::string& why) {
 
 }  // namespace
 
+void swe::set_last_error(const std::string& msg) { g_error = msg; }
+
 struct swe_world {
   int nx = 0, nz = 0;
   long n = 0;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 #include "swe_types.h"
 
@@ -13,6 +14,9 @@ namespace swe {
 struct Fields {
   float* f[9];
 };
+
+// The calling thread's error message, read by swe_last_error (swe_capi.cu).
+void set_last_error(const std::string& msg);
 
 // ---- exact modes (swe_exact.cu) ----
 void launch_reset_tracks(const Fields& F, long n, cudaStream_t s);
