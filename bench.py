@@ -283,14 +283,16 @@ def run_ours(args):
     value = cycles_total / (total_ms / 1e3)
     ms_per_step = total_ms / args.steps
 
-    # Roofline of the step kernels (fly + cascade passes): algorithmic bytes
-    # per particle-step B = 76 + 16 k (3x3 height gather 36, four track
-    # read-modify-writes 32, the cell's exchange read-modify-write 8, 16 per
-    # cascade transfer), k = transfers per particle-step.
+    # Roofline of the dominant kernel. One erode cycle is one launch of the
+    # persistent kernel k_par_cycle, so its duration per launch is the
+    # event-timed cycle. Algorithmic bytes per particle-step B = 76 + 16 k
+    # (3x3 height gather 36, four track read-modify-writes 32, the cell's
+    # exchange read-modify-write 8, 16 per cascade transfer), k = transfers
+    # per particle-step; bytes per launch = B x particle-steps per cycle.
     k = transfers / max(psteps, 1)
     bytes_per_step = 76.0 + 16.0 * k
-    kernel_ms = fly_ms + cas_ms
-    achieved = bytes_per_step * psteps / (kernel_ms / 1e3) / 1e9
+    psteps_per_launch = psteps / args.steps
+    achieved = bytes_per_step * psteps_per_launch / (ms_per_step / 1e3) / 1e9
     peak, peak_note = FALLBACK_HBM_GBS, "fallback"
     try:
         peak = float(json.loads(PEAKS_FILE.read_text())["hbm_gbs"])
@@ -302,13 +304,12 @@ def run_ours(args):
     if tfile.exists():
         try:
             tj = json.loads(tfile.read_text())
-            traffic = tj.get("bytes_per_particle_step", None)
-            if traffic is not None:
-                traffic = traffic * psteps / args.steps
+            if int(tj.get("size", 0)) == args.size and int(tj.get("particles", 0)) == particles:
+                traffic = float(tj["dram_bytes_per_launch"])
         except Exception:
             traffic = None
 
-    per_cycle_launches = 2 + (params.max_age + 2) * (1 + 4)
+    per_cycle_launches = 1  # k_par_cycle
     line = {
         "metric": METRIC,
         "value": value,
@@ -324,11 +325,12 @@ def run_ours(args):
         "data": "synthetic",
         "config": config_dict(args, particles),
         "particle_steps_per_s": psteps * world_size / (total_ms / 1e3),
-        "kernels": {"fly_ms_per_cycle": fly_ms / args.steps, "cascade_ms_per_cycle": cas_ms / args.steps,
-                    "k_transfers_per_step": k, "particle_steps_per_cycle": psteps / args.steps},
+        "kernels": {"k_par_cycle_ms": ms_per_step, "fly_phases_ms": fly_ms / args.steps,
+                    "cascade_phases_ms": cas_ms / args.steps, "k_transfers_per_step": k,
+                    "particle_steps_per_cycle": psteps_per_launch},
         "roofline": {
             "bound": "hbm",
-            "kernel": "step kernels k_par_fly + k_par_cascade",
+            "kernel": "k_par_cycle (one launch = one erode cycle)",
             "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",
