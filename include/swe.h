@@ -56,6 +56,7 @@ typedef struct swe_params {
   float mapscale;       /* 80    */
   float pspeed[3];      /* (1,0,0) */
   int frac_bits;        /* parallel mode: fixed-point fraction bits, 8..28 (24) */
+  int lanes;            /* parallel mode: particles in flight at once (0) */
 } swe_params;
 
 /* Per-cell fields, in the order of quad::cell (cellpool.h:226-240). */
@@ -76,14 +77,18 @@ typedef enum swe_field {
  *            (world.hpp:47-67), with the C library rand() sequence of
  *            srand(seed) (or a caller tape) and the C library's expf: the
  *            reference's results bit for bit. One GPU thread; a parity mode.
- *  PARALLEL: all particles of a cycle fly together in lock-step steps. In a
- *            step every particle flies against the heights as they were at
- *            the start of the step and adds its erosion/deposition to the
- *            map in fixed point; then the cascades the step owes run in a
- *            fixed conflict-free order (nine cell colours x%3, z%3). Mass is
- *            conserved exactly and the result does not depend on thread
- *            scheduling. Random numbers come from a counter-based generator
- *            keyed by (seed, cycle, particle, step). The throughput mode. */
+ *  PARALLEL: the particles of a cycle fly in lock-step steps, at most
+ *            `lanes` of them at a time; a lane whose particle dies takes the
+ *            cycle's next particle (lanes = 0: max(1024, nx*nz/64), which
+ *            keeps the terrain statistics of the sequential reference;
+ *            lanes < 0: all particles at once, fastest, statistically
+ *            further from the reference). In a step every particle flies
+ *            against the heights as they were at the start of the step and
+ *            adds its erosion/deposition to the map in fixed point; then the
+ *            cascades the step owes run in a fixed conflict-free order (nine
+ *            cell colours x%3, z%3). Mass is conserved exactly and the result
+ *            does not depend on thread scheduling. Random numbers come from a
+ *            counter-based generator keyed by (seed, cycle, particle, age). */
 typedef enum swe_mode { SWE_MODE_ORDERED = 0, SWE_MODE_PARALLEL = 1 } swe_mode;
 
 typedef struct swe_world swe_world;

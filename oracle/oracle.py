@@ -59,6 +59,7 @@ class _CParams(ctypes.Structure):
         ("mapscale", ctypes.c_float),
         ("pspeed", ctypes.c_float * 3),
         ("frac_bits", ctypes.c_int),
+        ("lanes", ctypes.c_int),
     ]
 
 
@@ -105,7 +106,7 @@ def _ptr(a: np.ndarray):
 
 
 def params_struct(max_age=512, boundarylayer=2.0, suspension=0.05, gravity=0.1, lrate=0.1, maxdiff=0.005,
-                  settling=1.0, mapscale=80.0, pspeed=(1.0, 0.0, 0.0), frac_bits=24) -> _CParams:
+                  settling=1.0, mapscale=80.0, pspeed=(1.0, 0.0, 0.0), frac_bits=24, lanes=0) -> _CParams:
     c = _CParams()
     c.max_age = max_age
     c.boundarylayer = boundarylayer
@@ -118,6 +119,7 @@ def params_struct(max_age=512, boundarylayer=2.0, suspension=0.05, gravity=0.1, 
     for i in range(3):
         c.pspeed[i] = pspeed[i]
     c.frac_bits = frac_bits
+    c.lanes = lanes
     return c
 
 

@@ -349,6 +349,7 @@ void so_params_default(so_params* p) {
   p->mapscale = 80.0f;
   p->pspeed[0] = 1.0f; p->pspeed[1] = 0.0f; p->pspeed[2] = 0.0f;
   p->frac_bits = 24;
+  p->lanes = 0;
 }
 
 so_world* so_create(int nx, int nz, const so_params* p) {
@@ -529,7 +530,8 @@ struct ParCtx {
 };
 
 // One step of one particle against the step-start heights; true if alive.
-bool par_fly(ParCtx& X, PState& P, int step) {
+// Turbulence draws are keyed by (particle, age after this step's increment).
+bool par_fly(ParCtx& X, PState& P) {
   so_world* w = X.w;
   const so_params& c = w->p;
   const int nx = w->nx, nz = w->nz;
@@ -573,7 +575,7 @@ bool par_fly(ParCtx& X, PState& P, int step) {
   const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
   sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
   uint32_t u[4];
-  so_philox4x32((uint32_t)P.id, (uint32_t)step, X.c_lo, X.c_hi, X.seed_lo, X.seed_hi, u);
+  so_philox4x32((uint32_t)P.id, (uint32_t)P.age, X.c_lo, X.c_hi, X.seed_lo, X.seed_hi, u);
   const float rx = (float)(int)(u[0] % 1001u), ry = (float)(int)(u[1] % 1001u), rz = (float)(int)(u[2] % 1001u);
   sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
   const float drag = 1.0f - 0.3f * sed;
@@ -673,6 +675,17 @@ void ensure_fixed(so_world* w) {
 
 extern "C" {
 
+int so_par_lanes(int lanes, int nx, int nz, int particles) {
+  long l;
+  if (lanes > 0) l = lanes;
+  else if (lanes == 0) {
+    l = (long)nx * nz / 64;
+    if (l < 1024) l = 1024;
+  } else l = particles;
+  if (l > particles) l = particles;
+  return (int)(l < 1 ? 1 : l);
+}
+
 void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_t* cycle_counter) {
   ensure_fixed(w);
   const size_t n = (size_t)w->nx * w->nz;
@@ -695,7 +708,9 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
     X.D = D.data();
     X.C = C.data();
     live.clear();
-    for (int i = 0; i < particles; i++) {
+    const int lanes = so_par_lanes(w->p.lanes, w->nx, w->nz, particles);
+    int next_id = 0;
+    auto spawn = [&](int i) {
       uint32_t u[4];
       so_philox4x32((uint32_t)i, 0xFFFFFFFFu, X.c_lo, X.c_hi, X.seed_lo, X.seed_hi, u);
       const int x = (int)(u[0] % (uint32_t)w->nx), z = (int)(u[1] % (uint32_t)w->nz);
@@ -705,12 +720,13 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
       P.px = (float)x + (float)fxq / 1000.0f; P.py = 0.0f; P.pz = (float)z + (float)fzq / 1000.0f;
       P.vx = P.vy = P.vz = 0.0f;
       live.push_back(P);
-    }
-    for (int step = 0; !live.empty(); step++) {
+    };
+    while (next_id < particles && (int)live.size() < lanes) spawn(next_id++);
+    while (!live.empty()) {
       X.H = w->hq.data();
       next.clear();
       for (PState& P : live) {
-        if (par_fly(X, P, step)) next.push_back(P);
+        if (par_fly(X, P)) next.push_back(P);
         else X.exported += P.sed_q;
       }
       if (!next.empty()) {
@@ -722,6 +738,8 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
         X.transfers += cascade_phase(w, H, C.data());
       }
       live.swap(next);
+      // freed lanes take the cycle's next particles; they fly from the next step
+      while (next_id < particles && (int)live.size() < lanes) spawn(next_id++);
     }
     for (size_t i = 0; i < n; i++) {
       for (int k = 0; k < 4; k++) {

@@ -30,6 +30,7 @@ typedef struct so_params {
   float mapscale;       /* quad::mapscale      cellpool.h:184 */
   float pspeed[3];      /* Wind::pspeed        wind.hpp:13 */
   int frac_bits;        /* parallel model: fixed-point fraction bits */
+  int lanes;            /* parallel model: particles in flight (0 auto, <0 all) */
 } so_params;
 
 enum { SO_RNG_LIBC = 0, SO_RNG_GLIBC = 1, SO_RNG_TAPE = 2 };
@@ -67,6 +68,9 @@ void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out);
 /* --- CPU model of the parallel fixed-point mode (bitwise model of the GPU
  *     kernels: same float operation order, same counter-based RNG). --- */
 void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_t* cycle_counter);
+/* Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/64),
+ * < 0 -> all particles of the cycle; never more than the cycle's particles. */
+int so_par_lanes(int lanes, int nx, int nz, int particles);
 void so_par_get_heights_q(so_world* w, int32_t* dst);
 void so_par_ledger(so_world* w, int64_t* map_q, int64_t* exported_q);
 void so_philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,

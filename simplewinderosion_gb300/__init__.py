@@ -64,6 +64,7 @@ class _CParams(ctypes.Structure):
         ("mapscale", ctypes.c_float),
         ("pspeed", ctypes.c_float * 3),
         ("frac_bits", ctypes.c_int),
+        ("lanes", ctypes.c_int),
     ]
 
 
@@ -73,7 +74,9 @@ class Params:
     Wind::maxAge/boundarylayer/suspension/gravity (wind.hpp:23-26),
     World::lrate/maxdiff/settling (world.hpp:30-32), quad::mapscale
     (cellpool.h:184), Wind::pspeed (wind.hpp:13). frac_bits is the parallel
-    mode's fixed-point resolution."""
+    mode's fixed-point resolution; lanes its particles in flight (0: automatic,
+    max(1024, cells/64), which keeps the sequential reference's terrain
+    statistics; < 0: all particles of a cycle at once)."""
 
     max_age: int = 512
     boundarylayer: float = 2.0
@@ -85,11 +88,12 @@ class Params:
     mapscale: float = 80.0
     pspeed: tuple = (1.0, 0.0, 0.0)
     frac_bits: int = 24
+    lanes: int = 0
 
     def to_c(self) -> _CParams:
         c = _CParams()
         for k in ("max_age", "boundarylayer", "suspension", "gravity", "lrate", "maxdiff", "settling",
-                  "mapscale", "frac_bits"):
+                  "mapscale", "frac_bits", "lanes"):
             setattr(c, k, getattr(self, k))
         for i in range(3):
             c.pspeed[i] = float(self.pspeed[i])

@@ -133,7 +133,7 @@ int use_device(swe_world* w) {
   return SWE_OK;
 }
 
-// Parallel-mode buffers, grown to hold `particles`.
+// Parallel-mode buffers, grown to hold `particles` in flight.
 int ensure_parallel(swe_world* w, int particles) {
   // heights, exchange deltas and visit counts, each padded to 64 elements
   // so every map starts 256-byte aligned (the apply phase uses int4).
@@ -190,10 +190,10 @@ int ensure_fixed(swe_world* w) {
 
 // Enqueue one parallel erode cycle: reset the grid barrier, then the
 // persistent cooperative kernel (spawn, steps, EMA).
-int enqueue_parallel_cycle(swe_world* w, int particles) {
+int enqueue_parallel_cycle(swe_world* w, int particles, int lanes) {
   SWE_CK(cudaMemsetAsync(w->gbar, 0, sizeof(swe::GridBarrier), w->stream));
-  SWE_CK(swe::launch_par_cycle(w->pb, w->F, w->consts(), w->seed, w->cnt, w->gbar, particles, w->cycle_grid,
-                               w->stream));
+  SWE_CK(swe::launch_par_cycle(w->pb, w->F, w->consts(), w->seed, w->cnt, w->gbar, particles, lanes,
+                               w->cycle_grid, w->stream));
   return SWE_OK;
 }
 
@@ -215,6 +215,7 @@ void swe_params_default(swe_params* p) {
   p->pspeed[1] = 0.0f;
   p->pspeed[2] = 0.0f;
   p->frac_bits = 24;
+  p->lanes = 0;
 }
 
 const char* swe_last_error(void) { return g_error.c_str(); }
@@ -366,11 +367,12 @@ int swe_world_erode(swe_world* w, int cycles, int particles, swe_mode mode) {
     w->hq_valid = false;
     return SWE_OK;
   }
-  if (int rc = ensure_parallel(w, particles)) return rc;
+  const int lanes = swe::par_lanes(w->p.lanes, w->nx, w->nz, particles);
+  if (int rc = ensure_parallel(w, lanes)) return rc;
   if (int rc = ensure_fixed(w)) return rc;
   SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, w->stream));
   for (int k = 0; k < cycles; k++)
-    if (int rc = enqueue_parallel_cycle(w, particles)) return rc;
+    if (int rc = enqueue_parallel_cycle(w, particles, lanes)) return rc;
   return SWE_OK;
 }
 

@@ -47,7 +47,10 @@ void launch_height_to_fixed(const float* height, int32_t* q, const Consts& c, Co
 int cycle_grid(int device);
 // One parallel erode cycle as one cooperative kernel.
 cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
-                             Counters* cnt, GridBarrier* gb, int particles, int grid, cudaStream_t s);
+                             Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s);
+// Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/64),
+// < 0 -> all particles of the cycle; never more than the cycle's particles.
+int par_lanes(int lanes, int nx, int nz, int particles);
 void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s);
 
 }  // namespace swe

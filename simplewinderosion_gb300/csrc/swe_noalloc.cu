@@ -104,7 +104,8 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
 
   const long n = (long)nx * nz;
   const size_t stride = ((size_t)n + 63) & ~(size_t)63;
-  const int cap = particles_per_cycle > 0 ? particles_per_cycle : 1;
+  const int lanes = swe::par_lanes(p->lanes, nx, nz, particles_per_cycle);
+  const int cap = lanes > 0 ? lanes : 1;
   unsigned char* base = ds->base;
   swe::Counters* cnt = reinterpret_cast<swe::Counters*>(base);
   swe::GridBarrier* gb = reinterpret_cast<swe::GridBarrier*>(base + kCountersBytes);
@@ -162,7 +163,7 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   SWE_NA_CK(cudaGetLastError());
   for (int k = 0; k < cycles; k++) {
     SWE_NA_CK(cudaMemsetAsync(gb, 0, sizeof(swe::GridBarrier), s));
-    SWE_NA_CK(swe::launch_par_cycle(B, F, c, seed, cnt, gb, particles_per_cycle, ds->grid, s));
+    SWE_NA_CK(swe::launch_par_cycle(B, F, c, seed, cnt, gb, particles_per_cycle, lanes, ds->grid, s));
   }
   if (status) {
     SWE_NA_CK(cudaStreamSynchronize(s));

@@ -3,14 +3,19 @@
 // One erode cycle (the World::erode(P) call, world.hpp:36-77) is ONE
 // persistent cooperative kernel, k_par_cycle, whose phases are separated by a
 // grid barrier:
-//   spawn     zero the track accumulators, spawn P particles
-//   per step (at most max_age + 2 steps, until no particle is alive):
+//   spawn     zero the track accumulators, spawn the first `lanes` of the
+//             cycle's P particles
+//   per step (until every particle of the cycle has flown):
 //     fly     every live particle runs Wind::fly (wind.hpp:28-117) against
 //             the heights as they were at the start of the step (nothing
 //             writes H in this phase). Its erosion/deposition exchange
 //             (wind.hpp:110-112) is added to the delta map D and the cascade
 //             it owes its cell (wind.hpp:114) to the visit map C, with integer
-//             atomics; survivors are compacted into the other particle buffer.
+//             atomics; survivors are compacted into the other particle buffer,
+//             and the lanes of the particles that died take the cycle's next
+//             particles (warp-cooperative spawning), which fly from the next
+//             step. Few lanes keep each flight on a nearly static map, as in
+//             the sequential reference; all P at once is fastest.
 //     colour  nine phases, cell colour (x%3, z%3). Colour 0 first adds the
 //             pending exchange deltas (H += D, D = 0) of the 3x3 block around
 //             each colour-0 cell; these blocks tile the map, so that is the
@@ -153,7 +158,8 @@ struct CycleArgs {
   uint32_t seed_lo, seed_hi;
   Counters* cnt;
   GridBarrier* gb;
-  int particles;
+  int particles;  // particles of the cycle
+  int lanes;      // particles in flight at once
 };
 
 // Per-thread tallies of the colour phases.
@@ -164,43 +170,61 @@ struct CascadeStats {
   unsigned int max_iters = 0;        // most cascades one cell ran in one step
 };
 
-// Spawn phase: zero the tracks, spawn particles uniformly in cells with a
-// 1/1000-quantised offset (world.hpp:52-54).
+// One particle at its spawn point: a uniform cell plus a 1/1000-quantised
+// offset (world.hpp:52-54), drawn from Philox counter (id, 0xFFFFFFFF, cycle).
+__device__ __forceinline__ void spawn_one(const CycleArgs& A, const ParticleSoA& S, int slot, int id, uint32_t c_lo,
+                                          uint32_t c_hi) {
+  const uint4 u = philox4x32((uint32_t)id, 0xFFFFFFFFu, c_lo, c_hi, A.seed_lo, A.seed_hi);
+  const int x = (int)(u.x % (uint32_t)A.c.nx);
+  const int z = (int)(u.y % (uint32_t)A.c.nz);
+  const int fxq = (int)(u.z % 1000u);
+  const int fzq = (int)(u.w % 1000u);
+  S.id[slot] = id;
+  S.age[slot] = 0;
+  S.px[slot] = (float)x + (float)fxq / 1000.0f;
+  S.py[slot] = 0.0f;
+  S.pz[slot] = (float)z + (float)fzq / 1000.0f;
+  S.vx[slot] = 0.0f; S.vy[slot] = 0.0f; S.vz[slot] = 0.0f;
+  S.sed_q[slot] = 0;
+}
+
+// Spawn phase: zero the tracks and spawn the first min(lanes, particles)
+// particles of the cycle.
 __device__ void spawn_phase(const CycleArgs& A, uint32_t c_lo, uint32_t c_hi) {
   const long n = (long)A.c.nx * A.c.nz;
-  const long total = n > A.particles ? n : A.particles;
+  const int first = A.lanes < A.particles ? A.lanes : A.particles;
+  const long total = n > first ? n : first;
   const ParticleSoA S = A.B.state[0];
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     if (i < n) {
       A.B.tq[0][i] = 0; A.B.tq[1][i] = 0; A.B.tq[2][i] = 0; A.B.tq[3][i] = 0;
     }
-    if (i < A.particles) {
-      const uint4 u = philox4x32((uint32_t)i, 0xFFFFFFFFu, c_lo, c_hi, A.seed_lo, A.seed_hi);
-      const int x = (int)(u.x % (uint32_t)A.c.nx);
-      const int z = (int)(u.y % (uint32_t)A.c.nz);
-      const int fxq = (int)(u.z % 1000u);
-      const int fzq = (int)(u.w % 1000u);
-      S.id[i] = (int)i;
-      S.age[i] = 0;
-      S.px[i] = (float)x + (float)fxq / 1000.0f;
-      S.py[i] = 0.0f;
-      S.pz[i] = (float)z + (float)fzq / 1000.0f;
-      S.vx[i] = 0.0f; S.vy[i] = 0.0f; S.vz[i] = 0.0f;
-      S.sed_q[i] = 0;
-    }
+    if (i < first) spawn_one(A, S, (int)i, (int)i, c_lo, c_hi);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    A.cnt->live[0] = A.particles;
+    A.cnt->live[0] = first;
     A.cnt->live[1] = 0;
+    A.cnt->refill[0] = 0;
+    A.cnt->refill[1] = 0;
+    A.cnt->next_id[0] = first;
+    A.cnt->next_id[1] = first;
     A.cnt->particles += (unsigned long long)A.particles;
   }
 }
 
-// Fly phase of one step: Wind::fly for every live particle against the
-// step-start heights.
-__device__ void fly_phase(const CycleArgs& A, int step, int count, uint32_t c_lo, uint32_t c_hi) {
+// Freed lanes take the cycle's next particles: ids id0 .. id0+k-1 go to
+// slots slot0 .. slot0+k-1 of state buffer `buf`; they fly from the next step.
+__device__ void refill_lanes(const CycleArgs& A, int buf, int slot0, int id0, int k, uint32_t c_lo, uint32_t c_hi) {
+  const ParticleSoA S = A.B.state[buf];
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x)
+    spawn_one(A, S, slot0 + j, id0 + j, c_lo, c_hi);
+}
+
+// Fly phase of one step: Wind::fly for every particle in flight against the
+// step-start heights; survivors are appended to the other state buffer.
+__device__ void fly_phase(const CycleArgs& A, int in, int count, uint32_t c_lo, uint32_t c_hi) {
   const Consts& c = A.c;
-  const int in = step & 1, outp = in ^ 1;
+  const int outp = in ^ 1;
   const ParticleSoA S = A.B.state[in];
   const ParticleSoA Dst = A.B.state[outp];
   const int32_t* H = A.B.hq;
@@ -262,7 +286,8 @@ __device__ void fly_phase(const CycleArgs& A, int step, int count, uint32_t c_lo
           if (collision < 0.0f) collision = 0.0f;
           const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
           sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
-          const uint4 u = philox4x32((uint32_t)id, (uint32_t)step, c_lo, c_hi, A.seed_lo, A.seed_hi);
+          // turbulence draws keyed by (particle, age after this step's increment)
+          const uint4 u = philox4x32((uint32_t)id, (uint32_t)age, c_lo, c_hi, A.seed_lo, A.seed_hi);
           const float rx = (float)(int)(u.x % 1001u), ry = (float)(int)(u.y % 1001u), rz = (float)(int)(u.z % 1001u);
           sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
           const float drag = 1.0f - 0.3f * sed;
@@ -663,18 +688,37 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
   lap(0);
 
   CascadeStats cst;
-  const int nsteps = A.c.max_age + 2;
-  for (int step = 0; step < nsteps; step++) {
-    const int count = ld_volatile(&cnt->live[step & 1]);
+  // Every step advances at least one particle, and each particle flies at
+  // most max_age + 2 steps: a loop bound that is never reached.
+  const long long max_steps = (long long)A.particles * (A.c.max_age + 2) + 2;
+  for (long long step = 0; step < max_steps; step++) {
+    const int in = (int)(step & 1), outp = in ^ 1;
+    const int count = ld_volatile(&cnt->live[in]) + ld_volatile(&cnt->refill[in]);
     if (count == 0) break;
-    fly_phase(A, step, count, c_lo, c_hi);
+    fly_phase(A, in, count, c_lo, c_hi);
     if (!grid_sync(A.gb, &cnt->status)) return;
     lap(1);
-    // Only survivors wrote D and C; with none, the map is already final.
-    const int survivors = ld_volatile(&cnt->live[(step + 1) & 1]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) cnt->live[step & 1] = 0;
-    if (survivors == 0) continue;
+    // Survivors and the particles that take the freed lanes; every block
+    // reads the same counters here and computes the same refill.
+    const int survivors = ld_volatile(&cnt->live[outp]);
+    const int nid = ld_volatile(&cnt->next_id[in]);
+    int refill = A.lanes - survivors;
+    if (refill > A.particles - nid) refill = A.particles - nid;
+    if (refill < 0) refill = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      cnt->live[in] = 0;
+      cnt->refill[outp] = refill;
+      cnt->next_id[outp] = nid + refill;
+    }
+    if (survivors == 0) {
+      // Only survivors wrote D and C: nothing to cascade.
+      if (refill == 0) break;
+      refill_lanes(A, outp, survivors, nid, refill, c_lo, c_hi);
+      if (!grid_sync(A.gb, &cnt->status)) return;
+      continue;
+    }
     for (int col = 0; col < 9; col++) {
+      if (col == 0) refill_lanes(A, outp, survivors, nid, refill, c_lo, c_hi);
       colour_phase(A, col / 3, col % 3, nb, list, owed, wcount, cst);
       if (!grid_sync(A.gb, &cnt->status)) return;
       lap(3 + col);
@@ -737,8 +781,22 @@ int cycle_grid(int device) {
   return sms * per_sm;
 }
 
+int par_lanes(int lanes, int nx, int nz, int particles) {
+  long l;
+  if (lanes > 0) {
+    l = lanes;
+  } else if (lanes == 0) {
+    l = (long)nx * nz / 64;
+    if (l < 1024) l = 1024;
+  } else {
+    l = particles;
+  }
+  if (l > particles) l = particles;
+  return (int)(l < 1 ? 1 : l);
+}
+
 cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
-                             Counters* cnt, GridBarrier* gb, int particles, int grid, cudaStream_t s) {
+                             Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s) {
   CycleArgs A;
   A.B = B;
   A.F = F;
@@ -748,6 +806,7 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   A.cnt = cnt;
   A.gb = gb;
   A.particles = particles;
+  A.lanes = lanes;
   void* args[] = {&A};
   return cudaLaunchCooperativeKernel((const void*)k_par_cycle, dim3(grid), dim3(kCycleThreads), args, 0, s);
 }

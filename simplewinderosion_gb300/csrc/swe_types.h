@@ -36,7 +36,9 @@ struct Counters {
   unsigned long long particles;
   unsigned long long transfers;
   long long exported_q;      // cumulative since the last height upload
-  int live[2];               // parallel mode: live particles per step parity
+  int live[2];               // parallel mode: survivors appended per step parity
+  int refill[2];             // parallel mode: particles spawned into freed lanes, per step parity
+  int next_id[2];            // parallel mode: next particle id to spawn, per step parity
   unsigned int status;       // SWE_STATUS_* bits
   unsigned int pad;
   long long tape_pos;        // ordered mode tape cursor

@@ -16,24 +16,26 @@ def _terrain(nx, nz, seed):
     return (terrain.normalise(terrain.fbm(nx, nz, seed, 4.0 / max(nx, nz))) + 0.1).astype(np.float32)
 
 
-def _pair(nx, nz, seed, wind=WIND_101, frac_bits=24, wseed=5):
+def _pair(nx, nz, seed, wind=WIND_101, frac_bits=24, wseed=5, lanes=0):
     h = _terrain(nx, nz, seed)
-    port = oracle.Port(nx, nz, pspeed=wind, frac_bits=frac_bits)
+    port = oracle.Port(nx, nz, pspeed=wind, frac_bits=frac_bits, lanes=lanes)
     port.set_field(0, h)
-    w = swe.World(nx, nz, params=swe.Params(pspeed=wind, frac_bits=frac_bits), seed=wseed)
+    w = swe.World(nx, nz, params=swe.Params(pspeed=wind, frac_bits=frac_bits, lanes=lanes), seed=wseed)
     w.upload(swe.Field.HEIGHT, h)
     return port, w
 
 
-@pytest.mark.parametrize("nx,nz,particles,cycles,wind,frac_bits", [
-    (16, 16, 64, 3, WIND_101, 24),
-    (33, 70, 900, 2, (0.0, 0.0, -1.0), 24),
-    (64, 64, 4096, 2, WIND_101, 16),
-    (96, 64, 6144, 2, (1.0, 0.0, 0.0), 28),
-    (128, 128, 16384, 2, WIND_101, 24),
+@pytest.mark.parametrize("nx,nz,particles,cycles,wind,frac_bits,lanes", [
+    (16, 16, 64, 3, WIND_101, 24, 0),
+    (33, 70, 900, 2, (0.0, 0.0, -1.0), 24, 0),
+    (64, 64, 4096, 2, WIND_101, 16, 0),
+    (96, 64, 6144, 2, (1.0, 0.0, 0.0), 28, -1),
+    (128, 128, 16384, 2, WIND_101, 24, 0),
+    (128, 128, 16384, 1, WIND_101, 16, -1),
+    (48, 40, 3000, 2, (0.0, 0.0, 1.0), 24, 37),
 ])
-def test_parallel_bitwise_vs_cpu_model(nx, nz, particles, cycles, wind, frac_bits):
-    port, w = _pair(nx, nz, 7, wind, frac_bits)
+def test_parallel_bitwise_vs_cpu_model(nx, nz, particles, cycles, wind, frac_bits, lanes):
+    port, w = _pair(nx, nz, 7, wind, frac_bits, lanes=lanes)
     port.par_erode(particles, cycles, seed=5)
     w.erode(particles, cycles, mode=swe.Mode.PARALLEL)
     for f in swe.FIELDS:
