@@ -5,17 +5,22 @@ map of seeded fBm (improved Perlin noise, base frequency 1/256, 8 octaves,
 in [0, 0.5]) plus a 0.1 +- 0.02 sediment layer and a square bedrock pyramid
 (height 0.4, base 200 cells) at the centre; prevailing wind
 normalize(1,0,1); 1,048,576 particles per erode cycle; parallel fixed-point
-mode with int32 Q16.16 heights. One bench step = one erode cycle
-(World::erode(P), source/world.hpp:36-77). Synthetic seeded data.
+mode with int32 Q16.16 heights and the default number of particles in flight
+(cells/64 = 16,384 lanes at 1024^2, the setting whose height histogram and
+spectrum match the sequential reference). One bench step = one erode cycle
+(World::erode(P), source/world.hpp:36-77). Synthetic seeded data. The same
+workload with all particles of a cycle in flight at once (faster, but its
+statistics drift from the reference's) is reported beside it.
 
 Timing: W untimed warm-up cycles, then K cycles, each bracketed by CUDA
 events on the world's stream; L2 is flushed (256 MiB write) before every
 timed cycle, outside the events. Multi-GPU (torchrun): one independent
 replica world per rank (the map does not shard), barrier + max over ranks.
 
-Also reported: kernel roofline (fly + cascade kernels, CUDA events inside
-the cycle graph), a CPU baseline (the oracle, bounded sample, one core),
-end-to-end cycles/s through the C ABI with pinned host buffers, and clocks.
+Also reported: the roofline of the dominant kernel, a CPU baseline (the
+reference's own code compiled here, else the oracle port; bounded sample,
+one core), end-to-end cycles/s through the C ABI with pinned host buffers,
+and clocks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -37,7 +42,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "erode cycles/s at 1024^2 (parallel GPU mode)"
+METRIC = "erode cycles/s at 1024^2 (plain GPU method, parallel fixed-point mode)"
 UNIT = "cycles/s"
 L2_FLUSH_BYTES = 256 << 20
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
@@ -53,6 +58,9 @@ def parse_args():
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--particles", type=int, default=0, help="particles per cycle (default size^2)")
     ap.add_argument("--frac-bits", type=int, default=16)
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="particles in flight: 0 = default (cells/64, min 1024), -1 = all at once")
+    ap.add_argument("--no-all-at-once", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=65536, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -68,7 +76,28 @@ def workload(size: int):
     return h, wind
 
 
+def effective_lanes(lanes: int, size: int, particles: int) -> int:
+    """Particles in flight for swe_params.lanes (the library's rule)."""
+    if lanes > 0:
+        lv = lanes
+    elif lanes == 0:
+        lv = max(1024, size * size // 64)
+    else:
+        lv = particles
+    return max(1, min(lv, particles))
+
+
+def kernel_form(lanes: int, sms: int = 152) -> tuple[str, int]:
+    """(dominant kernel, its launches per cycle) for `lanes` in flight."""
+    if lanes <= 4096:
+        return "k_par_lanes (one 16-CTA cluster)", 3
+    if lanes <= sms * 256 * 4:
+        return "k_par_lanes (one CTA per SM, cooperative)", 3
+    return "k_par_cycle (colour phases, cooperative)", 1
+
+
 def config_dict(args, particles):
+    lanes = effective_lanes(args.lanes, args.size, particles)
     return {
         "workload": f"plain method {args.size}^2: fBm(1/256)+sediment+pyramid(0.4, base 200), "
                     f"{particles} particles/cycle, wind normalize(1,0,1), parallel fixed-point "
@@ -77,6 +106,8 @@ def config_dict(args, particles):
         "particles_per_cycle": particles,
         "max_age": 512,
         "frac_bits": args.frac_bits,
+        "lanes": lanes,
+        "lanes_rule": "cells/64 (min 1024)" if args.lanes == 0 else ("all at once" if args.lanes < 0 else "given"),
         "l2": "flushed (256 MiB write) before every timed cycle",
         "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
     }
@@ -236,7 +267,10 @@ def run_ours(args):
     size = args.size
     particles = args.particles or size * size
     h, wind = workload(size)
-    params = swe.Params(pspeed=wind, frac_bits=args.frac_bits)
+    params = swe.Params(pspeed=wind, frac_bits=args.frac_bits, lanes=args.lanes)
+    lanes = effective_lanes(args.lanes, size, particles)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    kernel_name, launches_per_cycle = kernel_form(lanes, sms)
     w = swe.World(size, params=params, seed=1000 + rank)
     w.upload(swe.Field.HEIGHT, h)
     stream = torch.cuda.ExternalStream(w.stream(), device=dev)
@@ -284,7 +318,8 @@ def run_ours(args):
     ms_per_step = total_ms / args.steps
 
     # Roofline of the dominant kernel. One erode cycle is one launch of the
-    # persistent kernel k_par_cycle, so its duration per launch is the
+    # persistent step kernel (with, in the bounded-lanes forms, a map sweep
+    # before and after it), so its duration per launch is taken as the
     # event-timed cycle. Algorithmic bytes per particle-step B = 76 + 16 k
     # (3x3 height gather 36, four track read-modify-writes 32, the cell's
     # exchange read-modify-write 8, 16 per cascade transfer), k = transfers
@@ -304,12 +339,12 @@ def run_ours(args):
     if tfile.exists():
         try:
             tj = json.loads(tfile.read_text())
-            if int(tj.get("size", 0)) == args.size and int(tj.get("particles", 0)) == particles:
+            if (int(tj.get("size", 0)) == args.size and int(tj.get("particles", 0)) == particles
+                    and int(tj.get("lanes", 0)) == lanes):
                 traffic = float(tj["dram_bytes_per_launch"])
         except Exception:
             traffic = None
 
-    per_cycle_launches = 1  # k_par_cycle
     line = {
         "metric": METRIC,
         "value": value,
@@ -325,12 +360,12 @@ def run_ours(args):
         "data": "synthetic",
         "config": config_dict(args, particles),
         "particle_steps_per_s": psteps * world_size / (total_ms / 1e3),
-        "kernels": {"k_par_cycle_ms": ms_per_step, "fly_phases_ms": fly_ms / args.steps,
+        "kernels": {"cycle_ms": ms_per_step, "fly_phases_ms": fly_ms / args.steps,
                     "cascade_phases_ms": cas_ms / args.steps, "k_transfers_per_step": k,
                     "particle_steps_per_cycle": psteps_per_launch},
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_par_cycle (one launch = one erode cycle)",
+            "kernel": kernel_name,
             "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",
@@ -339,12 +374,15 @@ def run_ours(args):
             "bytes_per_particle_step": bytes_per_step,
             "traffic": traffic,
         },
-        "gpu_launches": per_cycle_launches * args.steps,
+        "gpu_launches": launches_per_cycle * args.steps,
         "clocks": clocks,
     }
 
     if not args.no_e2e:
         line["e2e"] = e2e(w, swe, torch, stream, h, particles, args, world_size)
+
+    if not args.no_all_at_once and args.lanes >= 0:
+        line["all_at_once"] = all_at_once(swe, torch, dev, h, wind, particles, args, world_size, rank)
 
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         v, kind, dt, steps = cpu_sample(size, h, wind, args.cpu_sample, particles, prefer_reference=True)
@@ -359,6 +397,43 @@ def run_ours(args):
     w.close()
     if world_size > 1:
         dist.destroy_process_group()
+
+
+def all_at_once(swe, torch, dev, h, wind, particles, args, world_size, rank):
+    """The same workload with every particle of a cycle in flight at once
+    (lanes = -1: the colour-phase kernel). Faster, but its height histogram
+    and spectrum drift from the sequential reference's."""
+    import torch.distributed as dist
+    params = swe.Params(pspeed=wind, frac_bits=args.frac_bits, lanes=-1)
+    w = swe.World(args.size, params=params, seed=1000 + rank)
+    w.upload(swe.Field.HEIGHT, h)
+    stream = torch.cuda.ExternalStream(w.stream(), device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        w.erode(particles, 1, mode=swe.Mode.PARALLEL)
+    torch.cuda.synchronize()
+    if world_size > 1:
+        dist.barrier()
+    total = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.erode(particles, 1, mode=swe.Mode.PARALLEL, sync=False)
+        e1.record(stream)
+        w.sync()
+        total += e0.elapsed_time(e1)
+    if world_size > 1:
+        t = torch.tensor([total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    w.close()
+    return {"value": args.steps * world_size / (total / 1e3), "unit": UNIT, "ms_per_step": total / args.steps,
+            "lanes": particles, "kernel": "k_par_cycle (colour phases, cooperative)",
+            "note": "all particles of a cycle in flight at once; mass conservation exact, but its height "
+                    "histogram and spectrum drift from the sequential reference's (not the headline)"}
 
 
 def e2e(w, swe, torch, stream, h, particles, args, world_size):

@@ -94,8 +94,9 @@ struct swe_world {
   int32_t* tape = nullptr;
   long long tape_len = 0;
   // parallel mode
-  int32_t* hq = nullptr;      // heights, exchange deltas, visit counts (3 padded maps)
+  int32_t* hq = nullptr;      // heights, exchange deltas, visit counts, cell stamps (4 padded maps)
   long long* tq = nullptr;    // 4n
+  unsigned long long* hw = nullptr;  // n height words of the cluster form
   void* pstate = nullptr;     // 2 buffers x 9 arrays x capacity
   int pcap = 0;
   swe::ParallelBuffers pb{};
@@ -135,13 +136,14 @@ int use_device(swe_world* w) {
 
 // Parallel-mode buffers, grown to hold `particles` in flight.
 int ensure_parallel(swe_world* w, int particles) {
-  // heights, exchange deltas and visit counts, each padded to 64 elements
-  // so every map starts 256-byte aligned (the apply phase uses int4).
+  // heights, exchange deltas, visit counts and cell stamps, each padded to
+  // 64 elements so every map starts 256-byte aligned.
   const size_t stride = ((size_t)w->n + 63) & ~(size_t)63;
   if (!w->hq) {
-    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 3 * stride));
-    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 3 * stride, w->stream));
+    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 4 * stride));
+    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 4 * stride, w->stream));
     SWE_CK(cudaMalloc(&w->tq, sizeof(long long) * 4 * w->n));
+    SWE_CK(cudaMalloc(&w->hw, sizeof(unsigned long long) * w->n));
     SWE_CK(cudaMemsetAsync(w->tq, 0, sizeof(long long) * 4 * w->n, w->stream));
     SWE_CK(cudaMalloc(&w->dsum, sizeof(long long)));
     SWE_CK(cudaMalloc(&w->gbar, sizeof(swe::GridBarrier)));
@@ -160,6 +162,8 @@ int ensure_parallel(swe_world* w, int particles) {
   B.hq = w->hq;
   B.dq = w->hq + stride;
   B.visits = w->hq + 2 * stride;
+  B.stamp = reinterpret_cast<uint32_t*>(w->hq + 3 * stride);
+  B.hw = w->hw;
   for (int k = 0; k < 4; k++) B.tq[k] = w->tq + (size_t)k * w->n;
   int32_t* base = reinterpret_cast<int32_t*>(w->pstate);
   for (int b = 0; b < 2; b++) {
@@ -287,6 +291,7 @@ void swe_world_destroy(swe_world* w) {
   cudaFree(w->tape);
   cudaFree(w->hq);
   cudaFree(w->tq);
+  cudaFree(w->hw);
   cudaFree(w->pstate);
   cudaFree(w->dsum);
   cudaFree(w->gbar);

@@ -36,6 +36,8 @@ struct ParallelBuffers {
   int32_t* hq;         // fixed-point heights
   int32_t* dq;         // exchange deltas pending for the cascade passes (zero between steps)
   int32_t* visits;     // cascades owed per cell (zero between steps)
+  uint32_t* stamp;     // cluster form: per cell, the step (from 1) in which it was last visited
+  unsigned long long* hw;  // cluster form: height words (fixed-point height, write tag)
   long long* tq[4];    // track accumulators (massflow, momx, momy, momz), 2^-32 units
   ParticleSoA state[2];
   int capacity;        // particles the state buffers hold

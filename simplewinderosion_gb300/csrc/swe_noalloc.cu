@@ -27,10 +27,12 @@ constexpr size_t kMaxCells = SWE_NOALLOC_MAX_CELLS;          // a multiple of 64
 constexpr size_t kMaxParticles = SWE_NOALLOC_MAX_PARTICLES;
 constexpr size_t kCountersBytes = align256(sizeof(swe::Counters));
 constexpr size_t kBarrierBytes = align256(sizeof(swe::GridBarrier));
-constexpr size_t kMapsBytes = 3 * kMaxCells * sizeof(int32_t);      // heights, deltas, owed cascades
+constexpr size_t kMapsBytes = 4 * kMaxCells * sizeof(int32_t);      // heights, deltas, owed cascades, stamps
 constexpr size_t kTracksBytes = 4 * kMaxCells * sizeof(long long);   // track accumulators
+constexpr size_t kWordsBytes = kMaxCells * sizeof(unsigned long long);  // height words
 constexpr size_t kParticleBytes = 2 * 9 * kMaxParticles * sizeof(int32_t);  // two state buffers
-constexpr size_t kScratchBytes = kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes + kParticleBytes;
+constexpr size_t kScratchBytes =
+    kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes + kWordsBytes + kParticleBytes;
 
 // The scratch. In host code this name is only a stand-in for the device
 // object: its device address comes from cudaGetSymbolAddress, per device.
@@ -111,12 +113,17 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   swe::GridBarrier* gb = reinterpret_cast<swe::GridBarrier*>(base + kCountersBytes);
   int32_t* maps = reinterpret_cast<int32_t*>(base + kCountersBytes + kBarrierBytes);
   long long* tracks = reinterpret_cast<long long*>(base + kCountersBytes + kBarrierBytes + kMapsBytes);
-  int32_t* pstate = reinterpret_cast<int32_t*>(base + kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes);
+  unsigned long long* words =
+      reinterpret_cast<unsigned long long*>(base + kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes);
+  int32_t* pstate = reinterpret_cast<int32_t*>(base + kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes +
+                                               kWordsBytes);
 
   swe::ParallelBuffers B{};
   B.hq = maps;
   B.dq = maps + stride;
   B.visits = maps + 2 * stride;
+  B.stamp = reinterpret_cast<uint32_t*>(maps + 3 * stride);
+  B.hw = words;
   for (int k = 0; k < 4; k++) B.tq[k] = tracks + (size_t)k * n;
   for (int b = 0; b < 2; b++) {
     int32_t* q = pstate + (size_t)b * 9 * cap;

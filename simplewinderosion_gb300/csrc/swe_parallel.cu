@@ -140,6 +140,39 @@ __device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
   return s_ok != 0;
 }
 
+// The same barrier with one arrival counter, for grids of one block per SM:
+// a single atomic per block, the last arrival releases the generation.
+__device__ bool grid_sync_flat(GridBarrier* gb, unsigned int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = ld_acquire(&gb->gen);
+    if (atom_add_acq_rel(&gb->count, 1u) == gridDim.x - 1) {
+      st_relaxed(&gb->count, 0u);
+      atom_add_release(&gb->gen, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire(&gb->gen) == g) {
+        if (ld_acquire(&gb->abort)) {
+          ok = 0;
+          break;
+        }
+        if (global_ns() - t0 > kBarrierLimitNs) {
+          atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
+          atomicExch(&gb->abort, 1u);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    if (ld_acquire(&gb->abort)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 __global__ void k_height_to_fixed(const float* __restrict__ H, int32_t* __restrict__ Q, Consts c, Counters* cnt) {
   const long n = (long)c.nx * c.nz;
   unsigned bad = 0;
@@ -163,12 +196,14 @@ struct CycleArgs {
 };
 
 // Per-thread tallies of the colour phases.
-struct CascadeStats {
-  unsigned long long transfers = 0;  // transfers that moved a non-zero amount
-  unsigned long long cascades = 0;   // World::cascade evaluations
-  unsigned long long cells = 0;      // cells with owed cascades
-  unsigned int max_iters = 0;        // most cascades one cell ran in one step
+template <class U>
+struct CascadeTally {
+  U transfers = 0;             // transfers that moved a non-zero amount
+  U cascades = 0;              // World::cascade evaluations
+  U cells = 0;                 // cells with owed cascades
+  unsigned int max_iters = 0;  // most cascades one cell ran in one step
 };
+using CascadeStats = CascadeTally<unsigned long long>;
 
 // One particle at its spawn point: a uniform cell plus a 1/1000-quantised
 // offset (world.hpp:52-54), drawn from Philox counter (id, 0xFFFFFFFF, cycle).
@@ -220,16 +255,114 @@ __device__ void refill_lanes(const CycleArgs& A, int buf, int slot0, int id0, in
     spawn_one(A, S, slot0 + j, id0 + j, c_lo, c_hi);
 }
 
+// One particle in flight.
+struct Particle {
+  int id, age, sed_q;
+  float px, py, pz, vx, vy, vz;
+};
+
+// Heights read by the fly step: an int32 map through L1 in the grid kernel;
+// in the cluster kernel the low halves of the 64-bit height words, from L2
+// (its cascades write the map from other SMs between steps).
+template <bool kWords>
+__device__ __forceinline__ int32_t load_h(const int32_t* H, long i) {
+  if constexpr (kWords) return __ldcg(H + 2 * i);
+  else return H[i];
+}
+
+// One Wind::fly step (wind.hpp:28-117) of particle p against the heights H
+// as they were at the start of the step. A survivor adds its tracks
+// (wind.hpp:93-96) and its exchange with the cell (wind.hpp:110-112) to the
+// accumulators, moves, and the index of the cell it flew from is returned;
+// the caller records the cascade it owes that cell (wind.hpp:114). A particle
+// that dies returns -1 and writes nothing (its sediment is exported).
+template <bool kWords>
+__device__ __forceinline__ long fly_particle(const Consts& c, const ParallelBuffers& B, const int32_t* H, uint32_t c_lo,
+                                             uint32_t c_hi, uint32_t seed_lo, uint32_t seed_hi, Particle& p,
+                                             unsigned& status) {
+  const int nx = c.nx, nz = c.nz;
+  const float inv = c.inv_scale;
+  const float sed = fx2f(p.sed_q, inv);
+  const bool inrange = fabsf(p.px) < 1073741824.0f && fabsf(p.pz) < 1073741824.0f;
+  const int ix = inrange ? (int)roundf(p.px) : -1;
+  const int iz = inrange ? (int)roundf(p.pz) : -1;
+  if (ix < 0 || iz < 0 || ix >= nx || iz >= nz) return -1;
+  const bool vx0 = ix > 0, vx2 = ix + 1 < nx, vz0 = iz > 0, vz2 = iz + 1 < nz;
+  const long ci = (long)ix * nz + iz;
+  // five unconditional loads (a missing neighbour reads the cell itself)
+  const int32_t q11 = load_h<kWords>(H, ci);
+  const int32_t q01 = load_h<kWords>(H, vx0 ? ci - nz : ci);
+  const int32_t q21 = load_h<kWords>(H, vx2 ? ci + nz : ci);
+  const int32_t q10 = load_h<kWords>(H, vz0 ? ci - 1 : ci);
+  const int32_t q12 = load_h<kWords>(H, vz2 ? ci + 1 : ci);
+  const float h11 = fx2f(q11, inv);
+  const float h01 = vx0 ? fx2f(q01, inv) : 0.0f;
+  const float h21 = vx2 ? fx2f(q21, inv) : 0.0f;
+  const float h10 = vz0 ? fx2f(q10, inv) : 0.0f;
+  const float h12 = vz2 ? fx2f(q12, inv) : 0.0f;
+
+  // quad::_normal (cellpool.h:200-223) on the step-start heights.
+  V3 n = v3(0.0f, 0.0f, 0.0f);
+  const V3 s = v3(1.0f, c.mapscale, 1.0f);
+  if (vx2 && vz2) n = add(n, cross(mulv(s, v3(0.0f, h12 - h11, 1.0f)), mulv(s, v3(1.0f, h21 - h11, 0.0f))));
+  if (vx0 && vz0) n = add(n, cross(mulv(s, v3(0.0f, h10 - h11, -1.0f)), mulv(s, v3(-1.0f, h01 - h11, 0.0f))));
+  if (vx2 && vz0) n = add(n, cross(mulv(s, v3(1.0f, h21 - h11, 0.0f)), mulv(s, v3(0.0f, h10 - h11, -1.0f))));
+  if (vx0 && vz2) n = add(n, cross(mulv(s, v3(-1.0f, h01 - h11, 0.0f)), mulv(s, v3(0.0f, h12 - h11, 1.0f))));
+  if (length(n) > 0.0f) n = normalize(n);
+
+  float py = p.py;
+  if (p.age == 0 || py < h11) py = h11;
+  if (p.age++ > c.max_age) return -1;
+  float hfac = expf_poly(-(py - h11) / c.boundarylayer);
+  if (hfac < 0.0f) hfac = 0.0f;
+  const V3 ps = v3(c.px, c.py, c.pz);
+  V3 sp = v3(p.vx, p.vy, p.vz);
+  float shadow = dot(normalize(ps), n);
+  if (shadow < 0.0f) shadow = 0.0f;
+  shadow = 1.0f - shadow;
+  sp = add(sp, smul(0.05f, sub(smul(0.1f + 0.9f * shadow, ps), sp)));
+  if (py > h11) sp.y -= c.gravity * sed;
+  float collision = -dot(normalize(sp), n);
+  if (collision < 0.0f) collision = 0.0f;
+  const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
+  sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
+  // turbulence draws keyed by (particle, age after this step's increment)
+  const uint4 u = philox4x32((uint32_t)p.id, (uint32_t)p.age, c_lo, c_hi, seed_lo, seed_hi);
+  const float rx = (float)(int)(u.x % 1001u), ry = (float)(int)(u.y % 1001u), rz = (float)(int)(u.z % 1001u);
+  sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
+  const float drag = 1.0f - 0.3f * sed;
+  sp = v3(sp.x * drag, sp.y * drag, sp.z * drag);
+  const float npx = p.px + sp.x, npy = py + sp.y, npz = p.pz + sp.z;
+
+  float force = -dot(normalize(sp), n) * length(sp);
+  if (force < 0.0f) force = 0.0f;
+  const float lift = (1.0f - collision) * length(sp);
+  const float capacity = force * hfac + 0.02f * lift * hfac;
+  const float diff = capacity - sed;
+  if (!(isfinite(diff) && isfinite(npx) && isfinite(npy) && isfinite(npz))) {
+    status |= 0x1u;  // SWE_STATUS_NONFINITE: retire the particle, no writes
+    return -1;
+  }
+  // Tracks of the pre-move cell (wind.hpp:93-96).
+  atomicAdd((unsigned long long*)&B.tq[0][ci], (unsigned long long)to_fixed64(sed * kTwo32));
+  atomicAdd((unsigned long long*)&B.tq[1][ci], (unsigned long long)to_fixed64(sp.x * kTwo32));
+  atomicAdd((unsigned long long*)&B.tq[2][ci], (unsigned long long)to_fixed64(sp.y * kTwo32));
+  atomicAdd((unsigned long long*)&B.tq[3][ci], (unsigned long long)to_fixed64(sp.z * kTwo32));
+  // Exchange with the cell (wind.hpp:110-112), in fixed point.
+  const int32_t ex_q = to_fixed(c.suspension * diff * c.scale);
+  atomicAdd(B.dq + ci, -ex_q);
+  p.sed_q = wrap_add(p.sed_q, ex_q);
+  p.px = npx; p.py = npy; p.pz = npz;
+  p.vx = sp.x; p.vy = sp.y; p.vz = sp.z;
+  return ci;
+}
+
 // Fly phase of one step: Wind::fly for every particle in flight against the
 // step-start heights; survivors are appended to the other state buffer.
 __device__ void fly_phase(const CycleArgs& A, int in, int count, uint32_t c_lo, uint32_t c_hi) {
-  const Consts& c = A.c;
   const int outp = in ^ 1;
   const ParticleSoA S = A.B.state[in];
   const ParticleSoA Dst = A.B.state[outp];
-  const int32_t* H = A.B.hq;
-  const int nx = c.nx, nz = c.nz;
-  const float inv = c.inv_scale;
 
   long long exported = 0;
   unsigned long long steps = 0;
@@ -241,87 +374,19 @@ __device__ void fly_phase(const CycleArgs& A, int in, int count, uint32_t c_lo, 
   for (int base = warp * 32; base < count; base += nwarps * 32) {
     const int i = base + lane;
     bool alive = false;
-    int id = 0, age = 0, sed_q = 0;
-    float px = 0, py = 0, pz = 0, vx = 0, vy = 0, vz = 0;
+    Particle p{};
     if (i < count) {
-      id = S.id[i]; age = S.age[i]; sed_q = S.sed_q[i];
-      px = S.px[i]; py = S.py[i]; pz = S.pz[i];
-      vx = S.vx[i]; vy = S.vy[i]; vz = S.vz[i];
-      const float sed = fx2f(sed_q, inv);
-      const bool inrange = fabsf(px) < 1073741824.0f && fabsf(pz) < 1073741824.0f;
-      const int ix = inrange ? (int)roundf(px) : -1;
-      const int iz = inrange ? (int)roundf(pz) : -1;
-      bool dies = ix < 0 || iz < 0 || ix >= nx || iz >= nz;
-      if (!dies) {
-        const bool vx0 = ix > 0, vx2 = ix + 1 < nx, vz0 = iz > 0, vz2 = iz + 1 < nz;
-        const long ci = (long)ix * nz + iz;
-        const float h11 = fx2f(H[ci], inv);
-        const float h01 = vx0 ? fx2f(H[ci - nz], inv) : 0.0f;
-        const float h21 = vx2 ? fx2f(H[ci + nz], inv) : 0.0f;
-        const float h10 = vz0 ? fx2f(H[ci - 1], inv) : 0.0f;
-        const float h12 = vz2 ? fx2f(H[ci + 1], inv) : 0.0f;
-
-        // quad::_normal (cellpool.h:200-223) on the step-start heights.
-        V3 n = v3(0.0f, 0.0f, 0.0f);
-        const V3 s = v3(1.0f, c.mapscale, 1.0f);
-        if (vx2 && vz2) n = add(n, cross(mulv(s, v3(0.0f, h12 - h11, 1.0f)), mulv(s, v3(1.0f, h21 - h11, 0.0f))));
-        if (vx0 && vz0) n = add(n, cross(mulv(s, v3(0.0f, h10 - h11, -1.0f)), mulv(s, v3(-1.0f, h01 - h11, 0.0f))));
-        if (vx2 && vz0) n = add(n, cross(mulv(s, v3(1.0f, h21 - h11, 0.0f)), mulv(s, v3(0.0f, h10 - h11, -1.0f))));
-        if (vx0 && vz2) n = add(n, cross(mulv(s, v3(-1.0f, h01 - h11, 0.0f)), mulv(s, v3(0.0f, h12 - h11, 1.0f))));
-        if (length(n) > 0.0f) n = normalize(n);
-
-        if (age == 0 || py < h11) py = h11;
-        if (age++ > c.max_age) dies = true;
-        if (!dies) {
-          float hfac = expf_poly(-(py - h11) / c.boundarylayer);
-          if (hfac < 0.0f) hfac = 0.0f;
-          const V3 ps = v3(c.px, c.py, c.pz);
-          V3 sp = v3(vx, vy, vz);
-          float shadow = dot(normalize(ps), n);
-          if (shadow < 0.0f) shadow = 0.0f;
-          shadow = 1.0f - shadow;
-          sp = add(sp, smul(0.05f, sub(smul(0.1f + 0.9f * shadow, ps), sp)));
-          if (py > h11) sp.y -= c.gravity * sed;
-          float collision = -dot(normalize(sp), n);
-          if (collision < 0.0f) collision = 0.0f;
-          const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
-          sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
-          // turbulence draws keyed by (particle, age after this step's increment)
-          const uint4 u = philox4x32((uint32_t)id, (uint32_t)age, c_lo, c_hi, A.seed_lo, A.seed_hi);
-          const float rx = (float)(int)(u.x % 1001u), ry = (float)(int)(u.y % 1001u), rz = (float)(int)(u.z % 1001u);
-          sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
-          const float drag = 1.0f - 0.3f * sed;
-          sp = v3(sp.x * drag, sp.y * drag, sp.z * drag);
-          const float npx = px + sp.x, npy = py + sp.y, npz = pz + sp.z;
-
-          float force = -dot(normalize(sp), n) * length(sp);
-          if (force < 0.0f) force = 0.0f;
-          const float lift = (1.0f - collision) * length(sp);
-          const float capacity = force * hfac + 0.02f * lift * hfac;
-          const float diff = capacity - sed;
-          if (!(isfinite(diff) && isfinite(npx) && isfinite(npy) && isfinite(npz))) {
-            status |= 0x1u;  // SWE_STATUS_NONFINITE: retire the particle, no writes
-            dies = true;
-          } else {
-            // Tracks of the pre-move cell (wind.hpp:93-96).
-            atomicAdd((unsigned long long*)&A.B.tq[0][ci], (unsigned long long)to_fixed64(sed * kTwo32));
-            atomicAdd((unsigned long long*)&A.B.tq[1][ci], (unsigned long long)to_fixed64(sp.x * kTwo32));
-            atomicAdd((unsigned long long*)&A.B.tq[2][ci], (unsigned long long)to_fixed64(sp.y * kTwo32));
-            atomicAdd((unsigned long long*)&A.B.tq[3][ci], (unsigned long long)to_fixed64(sp.z * kTwo32));
-            // Exchange with the cell (wind.hpp:110-112), in fixed point, and
-            // one cascade owed to the cell (wind.hpp:114).
-            const int32_t ex_q = to_fixed(c.suspension * diff * c.scale);
-            atomicAdd(A.B.dq + ci, -ex_q);
-            atomicAdd(A.B.visits + ci, 1);
-            sed_q = wrap_add(sed_q, ex_q);
-            px = npx; py = npy; pz = npz;
-            vx = sp.x; vy = sp.y; vz = sp.z;
-            alive = true;
-            steps++;
-          }
-        }
+      p.id = S.id[i]; p.age = S.age[i]; p.sed_q = S.sed_q[i];
+      p.px = S.px[i]; p.py = S.py[i]; p.pz = S.pz[i];
+      p.vx = S.vx[i]; p.vy = S.vy[i]; p.vz = S.vz[i];
+      const long ci = fly_particle<false>(A.c, A.B, A.B.hq, c_lo, c_hi, A.seed_lo, A.seed_hi, p, status);
+      if (ci >= 0) {
+        atomicAdd(A.B.visits + ci, 1);  // one cascade owed to the cell (wind.hpp:114)
+        alive = true;
+        steps++;
+      } else {
+        exported += p.sed_q;
       }
-      if (!alive) exported += sed_q;
     }
     // Compact survivors into the other buffer: one atomic per warp.
     const unsigned mask = __ballot_sync(0xffffffffu, alive);
@@ -330,9 +395,9 @@ __device__ void fly_phase(const CycleArgs& A, int in, int count, uint32_t c_lo, 
     slot0 = __shfl_sync(0xffffffffu, slot0, 0);
     if (alive) {
       const int o = slot0 + __popc(mask & ((1u << lane) - 1u));
-      Dst.id[o] = id; Dst.age[o] = age; Dst.sed_q[o] = sed_q;
-      Dst.px[o] = px; Dst.py[o] = py; Dst.pz[o] = pz;
-      Dst.vx[o] = vx; Dst.vy[o] = vy; Dst.vz[o] = vz;
+      Dst.id[o] = p.id; Dst.age[o] = p.age; Dst.sed_q[o] = p.sed_q;
+      Dst.px[o] = p.px; Dst.py[o] = p.py; Dst.pz[o] = p.pz;
+      Dst.vx[o] = p.vx; Dst.vy[o] = p.vy; Dst.vz[o] = p.vz;
     }
   }
   exported = warp_sum(exported);
@@ -413,6 +478,7 @@ __device__ __forceinline__ int cascade_general(int32_t* N, const bool (&val)[8],
   SWE_CE(1, 4) SWE_CE(3, 6)
   SWE_CE(2, 4) SWE_CE(3, 5)
   SWE_CE(3, 4)
+#undef SWE_CE
   int32_t hc = h0;
   int transfers = 0;
 #pragma unroll
@@ -501,6 +567,52 @@ __device__ __forceinline__ int cascade_unit(int32_t* N, const bool (&val)[8], fl
   return transfers;
 }
 
+// The cascades a cell owes (world.hpp:79-153, once per visit of the step,
+// stopping once a cascade moves nothing) on its 3x3 neighbourhood M, where
+// vx0/vx2/vz0/vz2 say whether the x-1, x+1, z-1, z+1 neighbours exist. The
+// common case takes the branch-free cascade: settling == 1 and the nine
+// heights (of in-bounds cells) within 2^24 steps of each other; cascades keep
+// every height inside the initial range.
+template <class Tally>
+__device__ __forceinline__ void cascade_cell(int32_t* M, bool vx0, bool vx2, bool vz0, bool vz2, int vis,
+                                             const CascadeConsts& kc, const Consts& c, Tally& st) {
+  const bool val[8] = {vx0 && vz0, vx0, vx0 && vz2, vz0, vz2, vx2 && vz0, vx2, vx2 && vz2};
+  int32_t lo = M[4], hi = M[4];
+  bool big = false;
+#pragma unroll
+  for (int s9 = 0; s9 < 9; s9++) {
+    const bool in = (s9 == 4) || val[s9 < 4 ? s9 : s9 - 1];
+    const int32_t h = M[s9];
+    if (in) {
+      lo = min(lo, h);
+      hi = max(hi, h);
+      big |= (h < 0 ? -h : h) >= (1 << 27);
+    }
+  }
+  const bool unit = kc.unit && !big && (long long)hi - (long long)lo < (1ll << 24);
+  int it = 0;
+  for (int r = 0; r < vis; r++) {
+    const int tr = unit ? cascade_unit(M, val, kc.hd1, kc.hd2)
+                        : (big ? cascade_general<long long>(M, val, kc, c) : cascade_general<int32_t>(M, val, kc, c));
+    it++;
+    if (tr == 0) break;
+    st.transfers += tr;
+  }
+  st.cascades += it;
+  st.cells += 1;
+  if ((unsigned)it > st.max_iters) st.max_iters = (unsigned)it;
+}
+
+__device__ __forceinline__ CascadeConsts cascade_consts(const Consts& c) {
+  CascadeConsts kc;
+  kc.md1 = 1.0f * c.maxdiff;
+  kc.md2 = kSqrt2 * c.maxdiff;
+  kc.hd1 = kc.md1 * (0.5f * c.scale);
+  kc.hd2 = kc.md2 * (0.5f * c.scale);
+  kc.unit = c.settling == 1.0f;
+  return kc;
+}
+
 // Colour phase: the owed cascades of every cell of colour (a, b).
 //
 // The 3x3 blocks around the colour-(0,0) cells tile the map (with virtual
@@ -523,12 +635,7 @@ __device__ void colour_phase(const CycleArgs& A, int a, int b, int32_t* nb, int*
   int32_t* H = A.B.hq;
   int32_t* Dq = A.B.dq;
   int32_t* V = A.B.visits;
-  CascadeConsts kc;
-  kc.md1 = 1.0f * c.maxdiff;
-  kc.md2 = kSqrt2 * c.maxdiff;
-  kc.hd1 = kc.md1 * (0.5f * c.scale);
-  kc.hd2 = kc.md2 * (0.5f * c.scale);
-  kc.unit = c.settling == 1.0f;
+  const CascadeConsts kc = cascade_consts(c);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   int32_t* N = nb + 9 * t;
   for (int base = blockIdx.x * blockDim.x; base < cells; base += gridDim.x * blockDim.x) {
@@ -601,34 +708,7 @@ __device__ void colour_phase(const CycleArgs& A, int a, int b, int32_t* nb, int*
       int32_t* M = nb + 9 * o;
       const int vis = owed[o];
       const bool vx0 = x > 0, vx2 = x + 1 < nx, vz0 = z > 0, vz2 = z + 1 < nz;
-      const bool val[8] = {vx0 && vz0, vx0, vx0 && vz2, vz0, vz2, vx2 && vz0, vx2, vx2 && vz2};
-      // The common case takes the branch-free cascade: settling == 1 and the
-      // nine heights (of in-bounds cells) within 2^24 steps of each other;
-      // cascades keep every height inside the initial range.
-      int32_t lo = M[4], hi = M[4];
-      bool big = false;
-#pragma unroll
-      for (int s9 = 0; s9 < 9; s9++) {
-        const bool in = (s9 == 4) || val[s9 < 4 ? s9 : s9 - 1];
-        const int32_t h = M[s9];
-        if (in) {
-          lo = min(lo, h);
-          hi = max(hi, h);
-          big |= (h < 0 ? -h : h) >= (1 << 27);
-        }
-      }
-      const bool unit = kc.unit && !big && (long long)hi - (long long)lo < (1ll << 24);
-      int it = 0;
-      for (int r = 0; r < vis; r++) {
-        const int tr = unit ? cascade_unit(M, val, kc.hd1, kc.hd2)
-                            : (big ? cascade_general<long long>(M, val, kc, c) : cascade_general<int32_t>(M, val, kc, c));
-        it++;
-        if (tr == 0) break;
-        st.transfers += (unsigned long long)tr;
-      }
-      st.cascades += (unsigned long long)it;
-      st.cells += 1;
-      if ((unsigned)it > st.max_iters) st.max_iters = (unsigned)it;
+      cascade_cell(M, vx0, vx2, vz0, vz2, vis, kc, c, st);
 #pragma unroll
       for (int u = 0; u < 3; u++) {
 #pragma unroll
@@ -752,6 +832,518 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
   }
 }
 
+// ---------------------------------------------------------------------------
+// Single-cluster form of the cycle, for a bounded number of particles in
+// flight.
+//
+// With few particles in flight a step is short, and the grid kernel's eleven
+// grid-wide barriers per step dominate it. Here one thread-block cluster of
+// 16 CTAs runs the steps of the cycle: each thread holds up to
+// kClusterMaxSlots lanes (particle state in shared memory), and a step has
+// two cluster barriers (hardware, a fraction of a microsecond):
+//   B1   every CTA's count of free lanes is read over distributed shared
+//        memory and the cycle's next particles take the free lanes (the same
+//        ids as in the grid kernel: the set of particles flying in a step is
+//        identical, only their lanes differ);
+//   fly  every particle flies against the step-start heights; the first
+//        particle to reach a cell in the step (its visit counter was 0) makes
+//        its thread the cell's owner and stamps the cell visited;
+//   B2   then each owner adds the cell's pending delta (H += D) and runs the
+//        cell's owed cascades.
+// The cascades are ordered cell by cell, reproducing the colour phases
+// exactly: two cascades interact only if their 3x3 neighbourhoods overlap
+// (cells at most 2 apart), and then the one of lower colour (x%3, z%3) runs
+// first; every delta is added before any cascade reads the cell. Heights live
+// here as 64-bit words, the fixed-point height in the low half and a tag in
+// the high half: 16*(step+1) + the number of writes the cell has had in the
+// step (its delta, then cascades). From the visited stamps of the 5x5 cells
+// around it, a cascade knows how many writes each cell of its 3x3 must have
+// had before it reads it (the cell's own delta if it was visited, and the
+// cascades of lower-colour visited cells next to it); it reads the words
+// until their tags say so, then writes each cell back with its tag plus one.
+// A value and its tag are written together by one 64-bit store, so the
+// ordering rests on the coherence of single words alone: no memory fences
+// (which serialise on an SM) are needed. Every wait is on a delta or on a
+// lower colour, so the waits cannot form a cycle; a thread handles its cells
+// in colour order, and the CTAs of a cluster are co-resident, so every wait
+// ends. Each wait still has a 2 s deadline: past it the thread sets
+// SWE_STATUS_TIMEOUT and the abort flag, tagged with the barrier count, and
+// every thread leaves the step loop after the same barrier.
+// ---------------------------------------------------------------------------
+constexpr int kClusterCtas = 16;
+constexpr int kClusterMaxThreads = 256;  // up to 255 registers a thread
+constexpr int kClusterMaxSlots = 4;
+constexpr int kLanesGridMaxThreads = 256;
+constexpr unsigned kClusterMaxSteps = 1u << 27;  // tags 16*(step+1)+k stay below 2^32
+
+__device__ __forceinline__ void cluster_barrier() {
+  // release/acquire at cluster scope (the defaults of arrive and wait)
+  asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Reads a 32-bit word of CTA `rank`'s shared memory at the address of `p`.
+__device__ __forceinline__ int ld_dsmem(const int* p, unsigned rank) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  unsigned ra;
+  int v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(ra) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v));
+}
+
+__device__ __forceinline__ int32_t word_height(unsigned long long w) { return (int32_t)(uint32_t)w; }
+__device__ __forceinline__ unsigned word_tag(unsigned long long w) { return (unsigned)(w >> 32); }
+__device__ __forceinline__ unsigned long long make_word(int32_t h, unsigned tag) {
+  return ((unsigned long long)tag << 32) | (uint32_t)h;
+}
+
+// Whether a cell word's tag shows exactly `want` writes in the step whose
+// tags start at `base` (want == 0: none, the tag is from an earlier step).
+__device__ __forceinline__ bool tag_ready(unsigned tag, unsigned base, unsigned want) {
+  return want ? tag == base + want : tag < base;
+}
+
+// Whether a thread gave up waiting before barrier number `ph` (the flag
+// holds the count of barriers its writer had passed, plus one).
+__device__ __forceinline__ bool aborted_before(GridBarrier* gb, unsigned ph) {
+  const unsigned a = ld_acquire(&gb->abort);
+  return a != 0 && a <= ph;
+}
+
+// Bit (du+2)*5 + (dw+2) for each cell of the 5x5 block around a cell; the
+// cells next to (qu, qw) (itself included).
+__host__ __device__ constexpr unsigned near_mask(int qu, int qw) {
+  unsigned m = 0;
+  for (int du = -2; du <= 2; du++)
+    for (int dw = -2; dw <= 2; dw++)
+      if (du - qu >= -1 && du - qu <= 1 && dw - qw >= -1 && dw - qw <= 1) m |= 1u << ((du + 2) * 5 + (dw + 2));
+  return m;
+}
+
+// kCluster: the 16 CTAs of one cluster (cluster barriers, lane counts over
+// distributed shared memory); otherwise one CTA per SM of a cooperative grid
+// (grid barriers, lane counts in global memory).
+template <bool kCluster>
+__global__ void __launch_bounds__(kCluster ? kClusterMaxThreads : kLanesGridMaxThreads, 1)
+    k_par_lanes(CycleArgs A, int slots) {
+  extern __shared__ int32_t dyn[];
+  __shared__ int s_free;               // free lanes of this CTA, read by the other CTAs
+  __shared__ int s_all[kClusterCtas];  // every CTA's free lanes, this step
+  __shared__ int s_warp[32];
+  __shared__ int s_sum[2][32];
+  __shared__ unsigned long long s_time[3];  // fly, cascades, last mark (CTA 0's thread 0)
+  const int T = blockDim.x;
+  const int cap = slots * T;
+  // Particle fields (id, age, sed_q, px, py, pz, vx, vy, vz) of lane slot j.
+  auto PI = [&](int f, int j) -> int32_t& { return dyn[f * cap + j]; };
+  auto PF = [&](int f, int j) -> float& { return reinterpret_cast<float*>(dyn)[f * cap + j]; };
+  int* s_own = dyn + 9 * cap;        // per lane slot: the cell it owns this step
+  int* s_vis = dyn + 10 * cap;       // per lane slot: cascades the owned cell owes
+  int32_t* N = dyn + 11 * cap + 9 * threadIdx.x;  // this thread's 3x3 neighbourhood
+
+  const Consts& c = A.c;
+  const ParallelBuffers& B = A.B;
+  unsigned long long* HW = B.hw;
+  Counters* cnt = A.cnt;
+  const int nx = c.nx, nz = c.nz;
+  const unsigned r = kCluster ? cluster_rank() : blockIdx.x;
+  const int nb = kCluster ? kClusterCtas : (int)gridDim.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
+  const unsigned long long cyc = cnt->cycle;
+  const uint32_t c_lo = (uint32_t)cyc, c_hi = (uint32_t)(cyc >> 32);
+  const CascadeConsts kc = cascade_consts(c);
+
+  // This CTA's share of the lanes; slot s of thread t is lane slot s*T+t.
+  const int L = A.lanes;
+  const int Lr = L / nb + ((int)r < L % nb ? 1 : 0);
+  unsigned lanes_mask = 0;
+#pragma unroll
+  for (int s = 0; s < kClusterMaxSlots; s++)
+    if (s < slots && s * T + t < Lr) lanes_mask |= 1u << s;
+  unsigned live = 0;
+
+  const bool timer = r == 0 && t == 0;
+  if (timer) {
+    s_time[0] = 0;
+    s_time[1] = 0;
+    s_time[2] = global_ns();
+  }
+
+  unsigned ph = 0;  // barriers passed
+  // 32-bit tallies, added to the counters before they could wrap
+  CascadeTally<unsigned> cst;
+  long long exported = 0;
+  unsigned steps = 0;
+  unsigned status = 0;
+  bool gave_up = false;
+  int nid = 0;  // next particle id of the cycle
+  // Every step advances a particle, and each flies at most max_age + 2 steps:
+  // a bound that is never reached (past it the cycle stops with
+  // SWE_STATUS_TIMEOUT).
+  const unsigned long long bound = (unsigned long long)A.particles * (c.max_age + 2) + 2;
+  const unsigned max_steps = bound > kClusterMaxSteps ? kClusterMaxSteps : (unsigned)bound;
+  unsigned step = 0;
+  for (;; step++) {
+    if (cst.transfers > 0x40000000u || cst.cascades > 0x40000000u || steps > 0x40000000u) {
+      atomicAdd(&cnt->transfers, (unsigned long long)cst.transfers);
+      atomicAdd(&cnt->cascades, (unsigned long long)cst.cascades);
+      atomicAdd(&cnt->particle_steps, (unsigned long long)steps);
+      cst.transfers = 0;
+      cst.cascades = 0;
+      steps = 0;
+    }
+    // Free lanes of this thread and their rank within the CTA.
+    const unsigned freem = lanes_mask & ~live;
+    const int f = __popc(freem);
+    int incl = f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int wpre = 0, btotal = 0;
+    for (int k = 0; k < nwarps; k++) {
+      const int v = s_warp[k];
+      wpre += k < warp ? v : 0;
+      btotal += v;
+    }
+    int total_free = 0, base = 0;
+    if constexpr (kCluster) {
+      if (t == 0) s_free = btotal;
+      cluster_barrier();  // B1: the last step's cascades are done everywhere
+      ph++;
+      if (timer) {
+        const unsigned long long now = global_ns();
+        s_time[1] += now - s_time[2];
+        s_time[2] = now;
+      }
+      if (aborted_before(A.gb, ph)) break;
+      if (t < kClusterCtas) s_all[t] = ld_dsmem(&s_free, (unsigned)t);
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kClusterCtas; k++) {
+        const int v = s_all[k];
+        total_free += v;
+        base += k < (int)r ? v : 0;
+      }
+    } else {
+      if (t == 0) A.gb->lanes_free[r] = btotal;
+      if (!grid_sync_flat(A.gb, &cnt->status)) break;  // B1
+      ph++;
+      if (timer) {
+        const unsigned long long now = global_ns();
+        s_time[1] += now - s_time[2];
+        s_time[2] = now;
+      }
+      int tot = 0, below = 0;
+      for (int k = t; k < nb; k += T) {
+        const int v = __ldcg(&A.gb->lanes_free[k]);
+        tot += v;
+        below += k < (int)r ? v : 0;
+      }
+      tot = warp_sum(tot);
+      below = warp_sum(below);
+      if (lane == 0) {
+        s_sum[0][warp] = tot;
+        s_sum[1][warp] = below;
+      }
+      __syncthreads();
+      for (int k = 0; k < nwarps; k++) {
+        total_free += s_sum[0][k];
+        base += s_sum[1][k];
+      }
+    }
+    const int survivors = L - total_free;
+    int refill = A.particles - nid;
+    if (refill > total_free) refill = total_free;
+    if (survivors == 0 && refill == 0) break;
+    if (step >= max_steps) {
+      status |= 0x8u;  // SWE_STATUS_TIMEOUT
+      break;
+    }
+
+    // The cycle's next particles take the free lanes (ids nid .. nid+refill-1).
+    int rank = base + wpre + (incl - f);
+#pragma unroll
+    for (int s = 0; s < kClusterMaxSlots; s++) {
+      if ((freem >> s) & 1u) {
+        if (rank < refill) {
+          const int id = nid + rank;
+          const uint4 u = philox4x32((uint32_t)id, 0xFFFFFFFFu, c_lo, c_hi, A.seed_lo, A.seed_hi);
+          const int j = s * T + t;
+          PI(0, j) = id;
+          PI(1, j) = 0;
+          PI(2, j) = 0;
+          PF(3, j) = (float)(int)(u.x % (uint32_t)nx) + (float)(int)(u.z % 1000u) / 1000.0f;
+          PF(4, j) = 0.0f;
+          PF(5, j) = (float)(int)(u.y % (uint32_t)nz) + (float)(int)(u.w % 1000u) / 1000.0f;
+          PF(6, j) = 0.0f; PF(7, j) = 0.0f; PF(8, j) = 0.0f;
+          live |= 1u << s;
+        }
+        rank++;
+      }
+    }
+    nid += refill;
+
+    // Fly.
+    const unsigned vmark = step + 1;     // visited stamp of this step
+    const unsigned tbase = 16u * vmark;  // tag base of this step
+    unsigned owned = 0;                  // bit s: slot s owns its cell this step
+#pragma unroll
+    for (int s = 0; s < kClusterMaxSlots; s++) {
+      if ((live >> s) & 1u) {
+        const int j = s * T + t;
+        Particle p;
+        p.id = PI(0, j); p.age = PI(1, j); p.sed_q = PI(2, j);
+        p.px = PF(3, j); p.py = PF(4, j); p.pz = PF(5, j);
+        p.vx = PF(6, j); p.vy = PF(7, j); p.vz = PF(8, j);
+        const long ci = fly_particle<true>(c, B, reinterpret_cast<const int32_t*>(HW), c_lo, c_hi, A.seed_lo,
+                                           A.seed_hi, p, status);
+        if (ci >= 0) {
+          steps++;
+          if (atomicAdd(B.visits + ci, 1) == 0) {
+            __stcg(B.stamp + ci, vmark);
+            s_own[j] = (int)ci;
+            owned |= 1u << s;
+          }
+          PI(1, j) = p.age; PI(2, j) = p.sed_q;
+          PF(3, j) = p.px; PF(4, j) = p.py; PF(5, j) = p.pz;
+          PF(6, j) = p.vx; PF(7, j) = p.vy; PF(8, j) = p.vz;
+        } else {
+          exported += p.sed_q;
+          live &= ~(1u << s);
+        }
+      }
+    }
+    if constexpr (kCluster) {
+      cluster_barrier();  // B2: every exchange and visit of the step is in
+      ph++;
+      if (aborted_before(A.gb, ph)) break;
+    } else {
+      if (!grid_sync_flat(A.gb, &cnt->status)) break;  // B2
+      ph++;
+    }
+    if (timer) {
+      const unsigned long long now = global_ns();
+      s_time[0] += now - s_time[2];
+      s_time[2] = now;
+    }
+
+    // The owned cells' deltas: the first write of each in the step.
+#pragma unroll
+    for (int s = 0; s < kClusterMaxSlots; s++) {
+      if ((owned >> s) & 1u) {
+        const int ci = s_own[s * T + t];
+        const int v = __ldcg(B.visits + ci);
+        const int32_t d = __ldcg(B.dq + ci);
+        const unsigned long long w = ld_relaxed64(HW + ci);
+        s_vis[s * T + t] = v;
+        __stcg(B.visits + ci, 0);
+        __stcg(B.dq + ci, 0);
+        st_relaxed64(HW + ci, make_word(wrap_add(word_height(w), d), tbase + 1));
+      }
+    }
+    // Cascades of the owned cells. Each lane takes its cells in colour order
+    // (lowest first) and cascades one as soon as the tags of its 3x3 words
+    // show every earlier write. The loop is warp-uniform: a lane whose cell
+    // is not ready yet polls again on the next pass instead of spinning, so
+    // a lane waiting for another lane of its own warp never holds that lane
+    // up. Every pass issues its loads in one batch.
+    {
+      unsigned todo = owned;  // slots whose cell still owes its cascades
+      int cs = -1;            // slot of the cell in hand
+      int ci = 0, x = 0, z = 0;
+      unsigned visited = 0, lower = 0, ready = 0, okmask = 0;
+      unsigned long long t_wait = 0;
+      for (;;) {
+        bool progressed = false;
+        bool fresh = false;  // a new cell in hand: its stamps were loaded in this pass
+        unsigned sv[25];
+        if (cs < 0 && todo && !gave_up) {
+          // the lowest-colour cell left
+          int best = 9;
+#pragma unroll
+          for (int s2 = 0; s2 < kClusterMaxSlots; s2++) {
+            if ((todo >> s2) & 1u) {
+              const int c2 = s_own[s2 * T + t];
+              const int x2 = c2 / nz, z2 = c2 - x2 * nz;
+              const int col2 = (x2 % 3) * 3 + z2 % 3;
+              if (col2 < best) {
+                best = col2;
+                cs = s2;
+              }
+            }
+          }
+          ci = s_own[cs * T + t];
+          x = ci / nz;
+          z = ci - x * nz;
+          // Stamps of the 5x5 block around (cells off the map read the
+          // cell's own stamp and are masked below).
+#pragma unroll
+          for (int k = 0; k < 25; k++) {
+            const int du = k / 5 - 2, dw = k % 5 - 2;
+            const bool in = x + du >= 0 && x + du < nx && z + dw >= 0 && z + dw < nz;
+            sv[k] = __ldcg(B.stamp + (in ? ci + du * nz + dw : ci));
+          }
+          okmask = 0;
+#pragma unroll
+          for (int u = 0; u < 3; u++)
+#pragma unroll
+            for (int w = 0; w < 3; w++)
+              if ((u == 0 ? x > 0 : (u == 2 ? x + 1 < nx : true)) && (w == 0 ? z > 0 : (w == 2 ? z + 1 < nz : true)))
+                okmask |= 1u << (3 * u + w);
+          ready = 0;
+          t_wait = 0;
+          fresh = true;
+        }
+        // The words not taken yet, loaded in the same batch as the stamps
+        // (taken or off-map words read the cell's own word and are masked).
+        unsigned long long wd[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          const int u = q / 3, w = q % 3;
+          const bool need = cs >= 0 && (((okmask & ~ready) >> q) & 1u);
+          wd[q] = cs >= 0 ? ld_relaxed64(HW + (need ? ci + (u - 1) * nz + (w - 1) : ci)) : 0ull;
+        }
+        if (fresh) {
+          // visited cells of the 5x5 block, and those of lower colour
+          const int xr = x % 3, zr = z % 3, col = xr * 3 + zr;
+          visited = 1u << 12;
+          lower = 0;
+#pragma unroll
+          for (int k = 0; k < 25; k++) {
+            const int du = k / 5 - 2, dw = k % 5 - 2;
+            const bool in = x + du >= 0 && x + du < nx && z + dw >= 0 && z + dw < nz;
+            const bool v = k != 12 && in && sv[k] == vmark;
+            const bool lo = ((xr + du + 3) % 3) * 3 + (zr + dw + 3) % 3 < col;
+            visited |= v ? 1u << k : 0u;
+            lower |= (v && lo) ? 1u << k : 0u;
+          }
+        }
+        if (cs >= 0) {
+          // Take the words whose tags show every earlier write (the cell's
+          // own delta if visited, the cascades of the lower-colour visited
+          // cells next to it).
+#pragma unroll
+          for (int q = 0; q < 9; q++) {
+            const int u = q / 3, w = q % 3;
+            const bool need = ((okmask & ~ready) >> q) & 1u;
+            const unsigned want = __popc(lower & near_mask(u - 1, w - 1)) + ((visited >> ((u + 1) * 5 + w + 1)) & 1u);
+            if (need && tag_ready(word_tag(wd[q]), tbase, want)) {
+              N[q] = word_height(wd[q]);
+              ready |= 1u << q;
+            }
+          }
+          if (ready == okmask) {
+            cascade_cell(N, x > 0, x + 1 < nx, z > 0, z + 1 < nz, s_vis[cs * T + t], kc, c, cst);
+            // Every cell of the neighbourhood takes its next tag, changed or not.
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+              const int u = q / 3, w = q % 3;
+              if ((okmask >> q) & 1u) {
+                const unsigned want =
+                    __popc(lower & near_mask(u - 1, w - 1)) + ((visited >> ((u + 1) * 5 + w + 1)) & 1u);
+                st_relaxed64(HW + ci + (u - 1) * nz + (w - 1), make_word(N[q], tbase + want + 1));
+              }
+            }
+            todo &= ~(1u << cs);
+            cs = -1;
+            progressed = true;
+          } else {
+            // Not ready: a deadline, and the abort flag of another thread.
+            const unsigned long long now = global_ns();
+            if (t_wait == 0) t_wait = now;
+            if (now - t_wait > kBarrierLimitNs || ld_volatile(reinterpret_cast<const int*>(&A.gb->abort)) != 0) {
+              if (!gave_up) {
+                status |= 0x8u;  // SWE_STATUS_TIMEOUT
+                atomicCAS(&A.gb->abort, 0u, ph + 1);
+              }
+              gave_up = true;
+              cs = -1;
+              todo = 0;
+            }
+          }
+        }
+        const bool more = cs >= 0 || (todo != 0 && !gave_up);
+        if (!__any_sync(0xffffffffu, more)) break;
+        if (!__any_sync(0xffffffffu, progressed)) __nanosleep(64);
+      }
+    }
+  }
+  // No CTA may leave while another can still read its shared memory.
+  if constexpr (kCluster) cluster_barrier();
+
+  // Tallies.
+  {
+    const unsigned long long tr = warp_sum((unsigned long long)cst.transfers);
+    const unsigned long long ca = warp_sum((unsigned long long)cst.cascades);
+    const unsigned long long ce = warp_sum((unsigned long long)cst.cells);
+    const long long ex = warp_sum(exported);
+    const unsigned long long stp = warp_sum((unsigned long long)steps);
+    const unsigned stt = __reduce_or_sync(0xffffffffu, status);
+    unsigned mi = cst.max_iters;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned other = __shfl_xor_sync(0xffffffffu, mi, o);
+      mi = other > mi ? other : mi;
+    }
+    if (lane == 0) {
+      if (tr) atomicAdd(&cnt->transfers, tr);
+      if (ca) atomicAdd(&cnt->cascades, ca);
+      if (ce) atomicAdd(&cnt->cascade_cells, ce);
+      if (mi) atomicMax(&cnt->max_cascade_iters, mi);
+      if (ex) atomicAdd((unsigned long long*)&cnt->exported_q, (unsigned long long)ex);
+      if (stp) atomicAdd(&cnt->particle_steps, stp);
+      if (stt) atomicOr(&cnt->status, stt);
+    }
+  }
+  if (timer) {
+    cnt->cycle = cyc + 1;
+    cnt->particles += (unsigned long long)A.particles;
+    cnt->fly_ns += s_time[0];
+    cnt->cascade_ns += s_time[1];
+    cnt->phase_ns[1] += s_time[0];
+    cnt->phase_ns[3] += s_time[1];
+  }
+}
+
+// Before a cluster-form cycle, on the whole GPU: height words with tag 0,
+// visited stamps and track accumulators cleared.
+__global__ void k_cluster_prologue(ParallelBuffers B, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    B.hw[i] = (unsigned long long)(uint32_t)B.hq[i];
+    B.stamp[i] = 0;
+    B.tq[0][i] = 0; B.tq[1][i] = 0; B.tq[2][i] = 0; B.tq[3][i] = 0;
+  }
+}
+
+// After it, on the whole GPU: heights back from the words, then tracks to
+// float, EMA, heights to float.
+__global__ void k_ema_cycle(CycleArgs A) {
+  const long n = (long)A.c.nx * A.c.nz;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    A.B.hq[i] = word_height(A.B.hw[i]);
+  ema_phase(A);
+}
+
 __global__ void k_sum_fixed(const int32_t* __restrict__ hq, long n, long long* out) {
   long long acc = 0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) acc += hq[i];
@@ -795,6 +1387,82 @@ int par_lanes(int lanes, int nx, int nz, int particles) {
   return (int)(l < 1 ? 1 : l);
 }
 
+namespace {
+
+// Bounded-lanes launch shapes. One cluster (16 CTAs) takes up to
+// kClusterMaxLanes lanes; beyond that one CTA per SM of a cooperative grid.
+// Threads per CTA are a multiple of 32 up to 256, with up to
+// kClusterMaxSlots lanes per thread.
+constexpr int kClusterMaxLanes = 4096;
+
+bool lanes_shape(int lanes, int ctas, int max_threads, int* threads, int* slots) {
+  const int per_cta = (lanes + ctas - 1) / ctas;
+  int t = (per_cta + 31) / 32 * 32;
+  if (t > max_threads) t = max_threads;
+  const int k = (per_cta + t - 1) / t;
+  if (k > kClusterMaxSlots) return false;
+  *threads = t;
+  *slots = k;
+  return true;
+}
+
+// particle state (9 words) and owned cell + owed cascades (2 words) per lane
+// slot, and a 3x3 neighbourhood per thread
+size_t lanes_smem(int threads, int slots) { return sizeof(int32_t) * (size_t)threads * (11 * slots + 9); }
+
+cudaError_t launch_cluster(const CycleArgs& A, int threads, int slots, cudaStream_t s, bool* launched) {
+  *launched = false;
+  const size_t smem = lanes_smem(threads, slots);
+  cudaError_t e = cudaFuncSetAttribute(k_par_lanes<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_par_lanes<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cudaSuccess;  // not available: the caller takes another form
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kClusterCtas);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kClusterCtas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, k_par_lanes<true>, &cfg) != cudaSuccess || clusters < 1) {
+    cudaGetLastError();
+    return cudaSuccess;
+  }
+  e = cudaLaunchKernelEx(&cfg, k_par_lanes<true>, A, slots);
+  *launched = e == cudaSuccess;
+  return e;
+}
+
+cudaError_t launch_lanes_grid(const CycleArgs& A, int ctas, int threads, int slots, cudaStream_t s,
+                              bool* launched) {
+  *launched = false;
+  const size_t smem = lanes_smem(threads, slots);
+  cudaError_t e = cudaFuncSetAttribute(k_par_lanes<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_par_lanes<false>, threads, smem);
+  if (e != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return cudaSuccess;
+  }
+  int sl = slots;
+  void* args[] = {const_cast<CycleArgs*>(&A), &sl};
+  e = cudaLaunchCooperativeKernel((const void*)k_par_lanes<false>, dim3(ctas), dim3(threads), args, smem, s);
+  *launched = e == cudaSuccess;
+  return e;
+}
+
+}  // namespace
+
 cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
                              Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s) {
   CycleArgs A;
@@ -807,6 +1475,26 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   A.gb = gb;
   A.particles = particles;
   A.lanes = lanes;
+  const long n = (long)c.nx * c.nz;
+  // Bounded lanes: one cluster, or one CTA per SM; cell indices are 32-bit there.
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms > 1024) sms = 1024;
+  int threads = 0, slots = 0;
+  const bool cluster = lanes <= kClusterMaxLanes;
+  if (n <= (1l << 30) && lanes_shape(lanes, cluster ? kClusterCtas : sms,
+                                     cluster ? kClusterMaxThreads : kLanesGridMaxThreads, &threads, &slots)) {
+    k_cluster_prologue<<<sweep_grid(n), 256, 0, s>>>(B, n);
+    bool launched = false;
+    const cudaError_t e = cluster ? launch_cluster(A, threads, slots, s, &launched)
+                                  : launch_lanes_grid(A, sms, threads, slots, s, &launched);
+    if (e != cudaSuccess) return e;
+    if (launched) {
+      k_ema_cycle<<<sweep_grid(n), 256, 0, s>>>(A);
+      return cudaGetLastError();
+    }
+  }
   void* args[] = {&A};
   return cudaLaunchCooperativeKernel((const void*)k_par_cycle, dim3(grid), dim3(kCycleThreads), args, 0, s);
 }

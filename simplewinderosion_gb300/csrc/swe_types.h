@@ -61,6 +61,7 @@ struct GridBarrier {
   unsigned int abort;  // set by a block that gave up waiting
   unsigned int pad[29];
   unsigned int leaf[16 * 32];  // block arrivals per leaf, one 128-byte line each
+  int lanes_free[1024];        // bounded-lanes kernel: free lanes per block, this step
 };
 
 // Particle state of the parallel mode, structure of arrays.

@@ -33,6 +33,12 @@ def _pair(nx, nz, seed, wind=WIND_101, frac_bits=24, wseed=5, lanes=0):
     (128, 128, 16384, 2, WIND_101, 24, 0),
     (128, 128, 16384, 1, WIND_101, 16, -1),
     (48, 40, 3000, 2, (0.0, 0.0, 1.0), 24, 37),
+    # bounded lanes on one CTA per SM, 1 and 2 lanes per thread, dense and sparse
+    (64, 64, 20000, 1, WIND_101, 16, -1),
+    (64, 64, 70000, 1, WIND_101, 24, -1),
+    (160, 96, 45000, 1, (0.0, 0.0, -1.0), 24, 40000),
+    # more lanes than that form holds: the colour-phase kernel
+    (64, 64, 200000, 1, WIND_101, 24, -1),
 ])
 def test_parallel_bitwise_vs_cpu_model(nx, nz, particles, cycles, wind, frac_bits, lanes):
     port, w = _pair(nx, nz, 7, wind, frac_bits, lanes=lanes)
