@@ -114,6 +114,36 @@ int swe_world_size(swe_world* w, int* nx, int* nz);
 int swe_world_upload(swe_world* w, swe_field f, const float* host, size_t n);
 int swe_world_download(swe_world* w, swe_field f, float* host, size_t n);
 
+/* An initial terrain, built on the device into SWE_HEIGHT (the other fields
+ * keep their values; like an upload of SWE_HEIGHT it resets the mass ledger).
+ * octaves == 0 gives the reference's own map::init terrain
+ * (cellpool.h:380-428): a Gaussian bump exp(-d^2 * nx * 0.2) around
+ * (nx/4, nz/2), normalised to [0, top] against min/max that include 0.
+ * octaves > 0 gives fractional Brownian motion of improved gradient noise
+ * (octave k at frequency base_freq * lacunarity^k with amplitude
+ * persistence^k; permutation and offsets drawn from splitmix64 seeded with
+ * `seed`), scaled to [0, top]. Then `npyramids` square pyramids of bedrock
+ * (cx, cz, height, base in cells: height at the centre, zero at base/2) are
+ * added, and `sediment` plus `sediment_jitter` times a uniform draw in
+ * [-1, 1) per cell. No counterpart beyond map::init: the reference's
+ * FastNoiseLite octave loop is commented out (cellpool.h:388-411). */
+typedef struct swe_terrain {
+  uint64_t seed;
+  int octaves;
+  float base_freq;
+  float lacunarity;
+  float persistence;
+  float top;
+  float sediment;
+  float sediment_jitter;
+  int npyramids;
+  const float* pyramids; /* host array, npyramids x 4 floats */
+} swe_terrain;
+
+/* The reference's terrain: the bump (octaves 0) in [0, 0.5], nothing added. */
+void swe_terrain_default(swe_terrain* t);
+int swe_world_terrain(swe_world* w, const swe_terrain* t);
+
 /* Device address of a field (nx*nz floats), for zero-copy callers. Valid until
  * swe_world_destroy; after a PARALLEL erode, SWE_HEIGHT holds the fixed-point
  * map converted back to float. */
@@ -123,6 +153,19 @@ int swe_world_device_field(swe_world* w, swe_field f, void** dev_ptr);
  * track reset, particle flights, EMA update of massflow/momentum. Asynchronous
  * on the world's stream. */
 int swe_world_erode(swe_world* w, int cycles, int particles_per_cycle, swe_mode mode);
+
+/* An ensemble: `cycles` PARALLEL erode cycles of worlds[i] with
+ * particles_per_cycle[i] particles each, for `count` independent worlds
+ * (sizes, seeds, winds and parameters of their own). Each world's result is
+ * the one swe_world_erode(worlds[i], cycles, particles_per_cycle[i],
+ * SWE_MODE_PARALLEL) gives. Worlds whose particles in flight fit one
+ * 16-CTA cluster (at most 16,384) run together in one persistent launch,
+ * each cluster taking the next world from a queue; the others run on their
+ * own streams. All worlds must live on one device and be distinct. Returns
+ * after the persistent launch has completed (the other worlds' cycles stay
+ * asynchronous on their streams). Extends the reference, which erodes one
+ * world (world.hpp:36-77). */
+int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle);
 
 /* Wait for the world's queued work; returns SWE_ERR_DEVICE if a kernel set a
  * status bit since the last call (bits in *status if non-NULL, then cleared). */
@@ -165,6 +208,20 @@ int swe_world_fly(swe_world* w, float x, float z, int steps, const int32_t* turb
 
 /* World::cascade at one cell (world.hpp:79-153), on the float height map. */
 int swe_world_cascade_at(swe_world* w, int x, int z);
+
+/* The surface vertices updatenode writes for rendering after each erode call
+ * (cellpool.h:302-333, SimpleWindErosion.cpp:219-221): per cell 12 floats,
+ * the position P = (x, mapscale*height, z), the normal (quad::_normal), and
+ * the edges T-P and B-P to the +x and +z neighbours (heights off the map
+ * read 0); n = 12*nx*nz floats in cell order written to host_out. A
+ * headless buffer in place of the reference's vertex pool. */
+int swe_world_vertices(swe_world* w, float* host_out, size_t n);
+
+/* The wind map the reference's app loop builds after each erode call
+ * (SimpleWindErosion.cpp:224-230): per cell the RGBA texel
+ * (0.5(1+erf(2 momentumx)), 0.5(1+erf(2 momentumy)), 0.5(1+erf(2 momentumz)), 1),
+ * 4*nx*nz floats in cell order written to host_rgba (n = 4*nx*nz). */
+int swe_world_windmap(swe_world* w, float* host_rgba, size_t n);
 
 /* Surface normal of every cell, quad::_normal (cellpool.h:200-223) as
  * map::normal calls it (cellpool.h:478-480): 3*nx*nz floats (x,y,z per cell)

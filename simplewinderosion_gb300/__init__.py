@@ -113,6 +113,13 @@ _P = ctypes.c_void_p
 _i64p = ctypes.POINTER(ctypes.c_int64)
 
 
+class _CTerrain(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("octaves", ctypes.c_int), ("base_freq", ctypes.c_float),
+                ("lacunarity", ctypes.c_float), ("persistence", ctypes.c_float), ("top", ctypes.c_float),
+                ("sediment", ctypes.c_float), ("sediment_jitter", ctypes.c_float), ("npyramids", ctypes.c_int),
+                ("pyramids", ctypes.POINTER(ctypes.c_float))]
+
+
 def _setup(L):
     L.swe_params_default.argtypes = [ctypes.POINTER(_CParams)]
     L.swe_world_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_CParams), ctypes.c_uint64,
@@ -124,6 +131,10 @@ def _setup(L):
     L.swe_world_download.argtypes = [_P, ctypes.c_int, _P, ctypes.c_size_t]
     L.swe_world_device_field.argtypes = [_P, ctypes.c_int, ctypes.POINTER(_P)]
     L.swe_world_erode.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.swe_world_terrain.argtypes = [_P, ctypes.POINTER(_CTerrain)]
+    L.swe_terrain_default.argtypes = [ctypes.POINTER(_CTerrain)]
+    L.swe_terrain_default.restype = None
+    L.swe_batch_erode.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.swe_world_sync.argtypes = [_P]
     L.swe_world_status.argtypes = [_P, ctypes.POINTER(ctypes.c_uint32)]
     L.swe_world_seed_rand.argtypes = [_P, ctypes.c_uint32]
@@ -135,6 +146,8 @@ def _setup(L):
                                 ctypes.POINTER(ctypes.c_int)]
     L.swe_world_cascade_at.argtypes = [_P, ctypes.c_int, ctypes.c_int]
     L.swe_world_normals.argtypes = [_P, _P, ctypes.c_size_t]
+    L.swe_world_windmap.argtypes = [_P, _P, ctypes.c_size_t]
+    L.swe_world_vertices.argtypes = [_P, _P, ctypes.c_size_t]
     L.swe_world_expf_bits.argtypes = [_P, ctypes.c_uint32, ctypes.c_size_t, _P]
     L.swe_world_get_stream.argtypes = [_P, ctypes.POINTER(_P)]
     L.swe_world_set_stream.argtypes = [_P, _P]
@@ -345,3 +358,44 @@ class World:
         out = np.empty(self.n * 3, dtype=np.float32)
         _check(lib.swe_world_normals(self._h, _ptr(out), out.size))
         return out.reshape(self.nx, self.nz, 3)
+
+    def vertices(self) -> np.ndarray:
+        """swe_world_vertices: [nx, nz, 12] floats per cell, the position,
+        normal and +x/+z edge vectors updatenode writes for rendering."""
+        out = np.empty(self.n * 12, dtype=np.float32)
+        _check(lib.swe_world_vertices(self._h, _ptr(out), out.size))
+        return out.reshape(self.nx, self.nz, 12)
+
+    def windmap(self) -> np.ndarray:
+        """swe_world_windmap: RGBA float texels [nx, nz, 4] of the momentum
+        fields, 0.5(1+erf(2 m)) per channel (the reference app's wind map)."""
+        out = np.empty(self.n * 4, dtype=np.float32)
+        _check(lib.swe_world_windmap(self._h, _ptr(out), out.size))
+        return out.reshape(self.nx, self.nz, 4)
+
+    def terrain(self, seed: int = 0, octaves: int = 0, base_freq: float = 1.0 / 64.0, lacunarity: float = 2.0,
+                persistence: float = 0.5, top: float = 0.5, sediment: float = 0.0, sediment_jitter: float = 0.0,
+                pyramids=()) -> None:
+        """swe_world_terrain: build the initial height map on the device
+        (octaves 0: the reference's Gaussian bump; else fBm), plus pyramids
+        (cx, cz, height, base) and a jittered sediment layer."""
+        pyr = np.ascontiguousarray(np.asarray(pyramids, dtype=np.float32).reshape(-1))
+        t = _CTerrain(seed & 0xFFFFFFFFFFFFFFFF, octaves, base_freq, lacunarity, persistence, top, sediment,
+                      sediment_jitter, len(pyr) // 4,
+                      pyr.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if len(pyr) else None)
+        _check(lib.swe_world_terrain(self._h, ctypes.byref(t)))
+
+
+def batch_erode(worlds, cycles: int, particles) -> None:
+    """swe_batch_erode: `cycles` PARALLEL erode cycles of every world of an
+    ensemble, particles[i] particles per cycle for worlds[i] (an int applies
+    to all). Each world ends as swe_world_erode would leave it; the worlds
+    that fit one 16-CTA cluster run together in one persistent launch."""
+    worlds = list(worlds)
+    if isinstance(particles, int):
+        particles = [particles] * len(worlds)
+    if len(particles) != len(worlds):
+        raise ValueError("one particle count per world")
+    handles = (_P * len(worlds))(*[w._h for w in worlds])
+    counts = (ctypes.c_int * len(worlds))(*[int(p) for p in particles])
+    _check(lib.swe_batch_erode(handles, len(worlds), int(cycles), counts))

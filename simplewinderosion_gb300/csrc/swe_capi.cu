@@ -2,6 +2,8 @@
 // device-resident cell maps and drives the kernels on its own stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -347,6 +349,41 @@ int swe_world_download(swe_world* w, swe_field f, float* host, size_t n) {
   return SWE_OK;
 }
 
+void swe_terrain_default(swe_terrain* t) {
+  if (!t) return;
+  std::memset(t, 0, sizeof(*t));
+  t->octaves = 0;
+  t->base_freq = 1.0f / 64.0f;
+  t->lacunarity = 2.0f;
+  t->persistence = 0.5f;
+  t->top = 0.5f;
+}
+
+int swe_world_terrain(swe_world* w, const swe_terrain* t) {
+  if (!w || !t) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (t->octaves < 0 || t->octaves > 32) return fail(SWE_ERR_INVALID, "octaves must be in [0, 32]");
+  if (t->npyramids < 0 || (t->npyramids > 0 && !t->pyramids))
+    return fail(SWE_ERR_INVALID, "npyramids must be >= 0 with a pyramid array");
+  if (t->octaves > 0 && !(t->base_freq > 0.0f)) return fail(SWE_ERR_INVALID, "base_freq must be > 0");
+  if (int rc = use_device(w)) return rc;
+  swe::TerrainSpec ts;
+  ts.seed = t->seed;
+  ts.octaves = t->octaves;
+  ts.base_freq = t->base_freq;
+  ts.lacunarity = t->lacunarity;
+  ts.persistence = t->persistence;
+  ts.top = t->top;
+  ts.sediment = t->sediment;
+  ts.sediment_jitter = t->sediment_jitter;
+  ts.npyramids = t->npyramids;
+  ts.pyramids = t->pyramids;
+  SWE_CK(swe::launch_terrain(w->F.f[SWE_HEIGHT], w->nx, w->nz, ts, w->stream));
+  w->hq_valid = false;
+  SWE_CK(cudaMemsetAsync(&w->cnt->exported_q, 0, sizeof(long long), w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  return SWE_OK;
+}
+
 int swe_world_device_field(swe_world* w, swe_field f, void** dev_ptr) {
   if (!w || !dev_ptr) return fail(SWE_ERR_INVALID, "NULL argument");
   if ((int)f < 0 || (int)f > 8) return fail(SWE_ERR_INVALID, "unknown field");
@@ -378,6 +415,67 @@ int swe_world_erode(swe_world* w, int cycles, int particles, swe_mode mode) {
   SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, w->stream));
   for (int k = 0; k < cycles; k++)
     if (int rc = enqueue_parallel_cycle(w, particles, lanes)) return rc;
+  return SWE_OK;
+}
+
+int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle) {
+  if (count < 0 || cycles < 0) return fail(SWE_ERR_INVALID, "count and cycles must be >= 0");
+  if (count == 0) return SWE_OK;
+  if (!worlds || !particles_per_cycle) return fail(SWE_ERR_INVALID, "NULL argument");
+  for (int i = 0; i < count; i++) {
+    if (!worlds[i]) return fail(SWE_ERR_INVALID, "a world is NULL");
+    if (particles_per_cycle[i] < 0) return fail(SWE_ERR_INVALID, "particles_per_cycle must be >= 0");
+    if (worlds[i]->device != worlds[0]->device) return fail(SWE_ERR_INVALID, "worlds on different devices");
+  }
+  {
+    std::vector<swe_world*> sorted(worlds, worlds + count);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(SWE_ERR_INVALID, "a world appears twice in the batch");
+  }
+  if (int rc = use_device(worlds[0])) return rc;
+  std::vector<swe::BatchWorld> fit;
+  std::vector<swe_world*> fit_w;
+  for (int i = 0; i < count; i++) {
+    swe_world* w = worlds[i];
+    const int particles = particles_per_cycle[i];
+    SWE_CK(cudaMemsetAsync(w->cnt, 0, 3 * sizeof(unsigned long long), w->stream));
+    if (cycles == 0) continue;
+    const int lanes = swe::par_lanes(w->p.lanes, w->nx, w->nz, particles);
+    if (int rc = ensure_parallel(w, lanes)) return rc;
+    if (int rc = ensure_fixed(w)) return rc;
+    SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, w->stream));
+    if (swe::batch_fits(lanes, w->nx, w->nz)) {
+      swe::BatchWorld b;
+      b.B = w->pb;
+      b.F = w->F;
+      b.c = w->consts();
+      b.seed = w->seed;
+      b.cnt = w->cnt;
+      b.gb = w->gbar;
+      b.particles = particles;
+      b.lanes = lanes;
+      fit.push_back(b);
+      fit_w.push_back(w);
+    } else {
+      for (int k = 0; k < cycles; k++)
+        if (int rc = enqueue_parallel_cycle(w, particles, lanes)) return rc;
+    }
+  }
+  if (fit.empty()) return SWE_OK;
+  // The persistent launch runs on the first batched world's stream, after
+  // the work already queued on every batched world's stream.
+  cudaStream_t s = fit_w[0]->stream;
+  for (size_t i = 1; i < fit_w.size(); i++) {
+    if (fit_w[i]->stream == s) continue;
+    cudaEvent_t ev;
+    SWE_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, fit_w[i]->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev, 0);
+    cudaEventDestroy(ev);
+    SWE_CK(e);
+  }
+  SWE_CK(swe::launch_par_batch(fit.data(), (int)fit.size(), cycles, s));
   return SWE_OK;
 }
 
@@ -554,6 +652,42 @@ int swe_world_normals(swe_world* w, float* host_out, size_t n) {
   };
   int rc = run();
   cudaFree(d_out);
+  return rc;
+}
+
+int swe_world_vertices(swe_world* w, float* host_out, size_t n) {
+  if (!w || !host_out) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (n != 12 * (size_t)w->n) return fail(SWE_ERR_INVALID, "n must equal 12*nx*nz");
+  if (int rc = use_device(w)) return rc;
+  float* d_out = nullptr;
+  auto run = [&]() -> int {
+    SWE_CK(cudaMallocAsync(&d_out, sizeof(float) * n, w->stream));
+    swe::launch_vertices(w->F.f[0], w->consts(), d_out, w->stream);
+    SWE_CK(cudaGetLastError());
+    SWE_CK(cudaMemcpyAsync(host_out, d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    return SWE_OK;
+  };
+  int rc = run();
+  if (d_out) cudaFreeAsync(d_out, w->stream);
+  return rc;
+}
+
+int swe_world_windmap(swe_world* w, float* host_rgba, size_t n) {
+  if (!w || !host_rgba) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (n != 4 * (size_t)w->n) return fail(SWE_ERR_INVALID, "n must equal 4*nx*nz");
+  if (int rc = use_device(w)) return rc;
+  float* d_out = nullptr;
+  auto run = [&]() -> int {
+    SWE_CK(cudaMallocAsync(&d_out, sizeof(float) * n, w->stream));
+    swe::launch_windmap(w->F, w->n, d_out, w->stream);
+    SWE_CK(cudaGetLastError());
+    SWE_CK(cudaMemcpyAsync(host_rgba, d_out, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream));
+    SWE_CK(cudaStreamSynchronize(w->stream));
+    return SWE_OK;
+  };
+  int rc = run();
+  if (d_out) cudaFreeAsync(d_out, w->stream);
   return rc;
 }
 

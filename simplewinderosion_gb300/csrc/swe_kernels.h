@@ -55,4 +55,41 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
 int par_lanes(int lanes, int nx, int nz, int particles);
 void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s);
 
+// ---- observables (swe_export.cu) ----
+// RGBA wind map of the momentum fields into out_rgba (4*n floats, device,
+// 16-byte aligned).
+void launch_windmap(const Fields& F, long n, float* out_rgba, cudaStream_t s);
+// Surface vertices of updatenode: 12 floats per cell (P, N, T-P, B-P).
+void launch_vertices(const float* height, const Consts& c, float* out, cudaStream_t s);
+
+// ---- initial terrains (swe_terrain.cu) ----
+struct TerrainSpec {
+  uint64_t seed;
+  int octaves;  // 0: the reference's Gaussian bump
+  double base_freq, lacunarity, persistence, top, sediment, sediment_jitter;
+  int npyramids;
+  const float* pyramids;  // host, npyramids x (cx, cz, height, base)
+};
+// Writes the terrain to `height` (nx*nz floats on the device); returns after
+// it is done.
+cudaError_t launch_terrain(float* height, int nx, int nz, const TerrainSpec& t, cudaStream_t s);
+
+// One world of an ensemble run by launch_par_batch.
+struct BatchWorld {
+  ParallelBuffers B;
+  Fields F;
+  Consts c;
+  uint64_t seed;
+  Counters* cnt;
+  GridBarrier* gb;
+  int particles;  // per cycle
+  int lanes;      // particles in flight (par_lanes)
+};
+// Whether a world with `lanes` in flight fits one cluster of the batch kernel.
+bool batch_fits(int lanes, int nx, int nz);
+// `cycles` parallel erode cycles of every world in one persistent launch of
+// 16-CTA clusters on stream s (the worlds' height maps already in fixed
+// point). Returns after the launch has completed.
+cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s);
+
 }  // namespace swe

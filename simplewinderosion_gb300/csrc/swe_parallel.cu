@@ -37,6 +37,8 @@
 // The grid barrier spins with an explicit deadline: a block that waits longer
 // than 2 s sets SWE_STATUS_TIMEOUT and an abort flag, and every block then
 // leaves the kernel at its next barrier, so the kernel always ends.
+#include <vector>
+
 #include "swe_device.cuh"
 #include "swe_kernels.h"
 
@@ -722,23 +724,46 @@ __device__ void colour_phase(const CycleArgs& A, int a, int b, int32_t* nb, int*
   }
 }
 
-// Tracks to float, EMA (world.hpp:70-76), heights to float.
-__device__ void ema_phase(const CycleArgs& A) {
+// Tracks to float, EMA (world.hpp:70-76), heights to float, for cells
+// i0, i0 + stride, ... With kWords the heights come from the cluster form's
+// height words and are written back to the fixed-point map too.
+template <bool kWords>
+__device__ void ema_cells(const CycleArgs& A, long i0, long stride) {
   const long n = (long)A.c.nx * A.c.nz;
   unsigned bad = 0;
   const float lrate = A.c.lrate;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  for (long i = i0; i < n; i += stride) {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const float t = __ll2float_rn(A.B.tq[k][i]) * kInvTwo32;
       A.F.f[5 + k][i] = t;
       A.F.f[1 + k][i] = (1.0f - lrate) * A.F.f[1 + k][i] + lrate * t;
     }
-    const int32_t q = A.B.hq[i];
+    int32_t q;
+    if constexpr (kWords) {
+      q = (int32_t)(uint32_t)A.B.hw[i];
+      A.B.hq[i] = q;
+    } else {
+      q = A.B.hq[i];
+    }
     if (q > 1073741823 || q < -1073741823) bad = 1;
     A.F.f[0][i] = fx2f(q, A.c.inv_scale);
   }
   if (bad) atomicOr(&A.cnt->status, 0x2u);
+}
+
+__device__ void ema_phase(const CycleArgs& A) {
+  ema_cells<false>(A, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
+}
+
+// Before a bounded-lanes cycle: height words with tag 0, visited stamps and
+// track accumulators cleared, for cells i0, i0 + stride, ...
+__device__ void prologue_cells(const ParallelBuffers& B, long n, long i0, long stride) {
+  for (long i = i0; i < n; i += stride) {
+    B.hw[i] = (unsigned long long)(uint32_t)B.hq[i];
+    B.stamp[i] = 0;
+    B.tq[0][i] = 0; B.tq[1][i] = 0; B.tq[2][i] = 0; B.tq[3][i] = 0;
+  }
 }
 
 __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(CycleArgs A) {
@@ -940,9 +965,7 @@ __host__ __device__ constexpr unsigned near_mask(int qu, int qw) {
 // distributed shared memory); otherwise one CTA per SM of a cooperative grid
 // (grid barriers, lane counts in global memory).
 template <bool kCluster>
-__global__ void __launch_bounds__(kCluster ? kClusterMaxThreads : kLanesGridMaxThreads, 1)
-    k_par_lanes(CycleArgs A, int slots) {
-  extern __shared__ int32_t dyn[];
+__device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32_t* dyn) {
   __shared__ int s_free;               // free lanes of this CTA, read by the other CTAs
   __shared__ int s_all[kClusterCtas];  // every CTA's free lanes, this step
   __shared__ int s_warp[32];
@@ -1325,23 +1348,66 @@ __global__ void __launch_bounds__(kCluster ? kClusterMaxThreads : kLanesGridMaxT
   }
 }
 
-// Before a cluster-form cycle, on the whole GPU: height words with tag 0,
-// visited stamps and track accumulators cleared.
-__global__ void k_cluster_prologue(ParallelBuffers B, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    B.hw[i] = (unsigned long long)(uint32_t)B.hq[i];
-    B.stamp[i] = 0;
-    B.tq[0][i] = 0; B.tq[1][i] = 0; B.tq[2][i] = 0; B.tq[3][i] = 0;
+template <bool kCluster>
+__global__ void __launch_bounds__(kCluster ? kClusterMaxThreads : kLanesGridMaxThreads, 1)
+    k_par_lanes(CycleArgs A, int slots) {
+  extern __shared__ int32_t dyn[];
+  lanes_cycle<kCluster>(A, slots, dyn);
+}
+
+// An ensemble of independent worlds in one persistent launch: each 16-CTA
+// cluster takes the next world from a queue and runs all of its cycles
+// (the map sweeps by the cluster's own threads, the steps as above), so
+// every world's result is the one a launch of its own would give.
+struct BatchItem {
+  CycleArgs A;
+  int slots;
+  int pad;
+};
+
+__global__ void __launch_bounds__(kClusterMaxThreads, 1)
+    k_par_batch(const BatchItem* __restrict__ items, int count, int cycles, unsigned* queue) {
+  extern __shared__ int32_t dyn[];
+  __shared__ int s_item;
+  __shared__ CycleArgs s_args;
+  __shared__ int s_slots;
+  const unsigned r = cluster_rank();
+  const int T = blockDim.x;
+  const long tid = (long)r * T + threadIdx.x, nthr = (long)kClusterCtas * T;
+  for (;;) {
+    if (r == 0 && threadIdx.x == 0) s_item = (int)atomicAdd(queue, 1u);
+    cluster_barrier();
+    const int item = ld_dsmem(&s_item, 0);
+    cluster_barrier();  // CTA 0 keeps its shared memory until every CTA has read it
+    if (item >= count) break;
+    // This world's arguments, copied to shared memory word by word.
+    {
+      const int* src = reinterpret_cast<const int*>(&items[item].A);
+      int* dst = reinterpret_cast<int*>(&s_args);
+      for (int k = threadIdx.x; k < (int)(sizeof(CycleArgs) / sizeof(int)); k += T) dst[k] = src[k];
+      if (threadIdx.x == 0) s_slots = items[item].slots;
+    }
+    __syncthreads();
+    const CycleArgs& A = s_args;
+    const long n = (long)A.c.nx * A.c.nz;
+    for (int k = 0; k < cycles; k++) {
+      if (r == 0 && threadIdx.x == 0) A.gb->abort = 0;
+      prologue_cells(A.B, n, tid, nthr);
+      cluster_barrier();
+      lanes_cycle<true>(A, s_slots, dyn);  // ends with a cluster barrier
+      ema_cells<true>(A, tid, nthr);         // the same cells per thread as the prologue
+    }
+    cluster_barrier();
   }
 }
 
-// After it, on the whole GPU: heights back from the words, then tracks to
-// float, EMA, heights to float.
+// The sweeps around a bounded-lanes cycle, on the whole GPU.
+__global__ void k_cluster_prologue(ParallelBuffers B, long n) {
+  prologue_cells(B, n, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
+}
+
 __global__ void k_ema_cycle(CycleArgs A) {
-  const long n = (long)A.c.nx * A.c.nz;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    A.B.hq[i] = word_height(A.B.hw[i]);
-  ema_phase(A);
+  ema_cells<true>(A, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
 }
 
 __global__ void k_sum_fixed(const int32_t* __restrict__ hq, long n, long long* out) {
@@ -1497,6 +1563,71 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   }
   void* args[] = {&A};
   return cudaLaunchCooperativeKernel((const void*)k_par_cycle, dim3(grid), dim3(kCycleThreads), args, 0, s);
+}
+
+bool batch_fits(int lanes, int nx, int nz) {
+  int threads = 0, slots = 0;
+  return (long)nx * nz <= (1l << 30) &&
+         lanes_shape(lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots);
+}
+
+cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s) {
+  if (count <= 0 || cycles <= 0) return cudaSuccess;
+  std::vector<BatchItem> items((size_t)count);
+  for (int i = 0; i < count; i++) {
+    const BatchWorld& w = worlds[i];
+    CycleArgs& A = items[i].A;
+    A.B = w.B;
+    A.F = w.F;
+    A.c = w.c;
+    A.seed_lo = (uint32_t)w.seed;
+    A.seed_hi = (uint32_t)(w.seed >> 32);
+    A.cnt = w.cnt;
+    A.gb = w.gb;
+    A.particles = w.particles;
+    A.lanes = w.lanes;
+    int threads = 0, slots = 0;
+    if (!lanes_shape(w.lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots)) return cudaErrorInvalidValue;
+    items[i].slots = slots;
+    items[i].pad = 0;
+  }
+  const size_t smem = lanes_smem(kClusterMaxThreads, kClusterMaxSlots);
+  cudaError_t e = cudaFuncSetAttribute(k_par_batch, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_par_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kClusterCtas);
+  cfg.blockDim = dim3(kClusterMaxThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kClusterCtas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  e = cudaOccupancyMaxActiveClusters(&clusters, k_par_batch, &cfg);
+  if (e != cudaSuccess) return e;
+  if (clusters < 1) return cudaErrorCooperativeLaunchTooLarge;
+  if (clusters > count) clusters = count;
+  cfg.gridDim = dim3(kClusterCtas * clusters);
+  // the items and the queue counter, freed in stream order after the launch
+  const size_t bytes = sizeof(BatchItem) * (size_t)count + 256;
+  void* d = nullptr;
+  e = cudaMallocAsync(&d, bytes, s);
+  if (e != cudaSuccess) return e;
+  BatchItem* d_items = reinterpret_cast<BatchItem*>(static_cast<char*>(d) + 256);
+  unsigned* d_queue = static_cast<unsigned*>(d);
+  e = cudaMemsetAsync(d_queue, 0, 256, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_items, items.data(), sizeof(BatchItem) * (size_t)count, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, k_par_batch, (const BatchItem*)d_items, count, cycles, d_queue);
+  // the host array must outlive the copy
+  const cudaError_t es = cudaStreamSynchronize(s);
+  cudaFreeAsync(d, s);
+  return e != cudaSuccess ? e : es;
 }
 
 void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s) {

@@ -113,3 +113,79 @@ def config_plain_large(seed: int = 2, n: int = 1024) -> np.ndarray:
     rs = np.random.RandomState((seed * 7919 + 1) & 0xFFFFFFFF)
     sed = 0.1 + 0.02 * rs.uniform(-1.0, 1.0, size=(n, n))
     return (bed + sed).astype(np.float32)
+
+
+# ---------------------------------------------------------------- device generator
+# The library builds terrains on the GPU (swe_world_terrain). Its random
+# draws come from splitmix64 (S. Vigna) instead of numpy's generator, and the
+# functions below restate its steps on the host, so the two agree to
+# rounding: the permutation by Fisher-Yates, two offsets, then one draw per
+# cell for the sediment jitter.
+_M64 = (1 << 64) - 1
+_GOLDEN = 0x9E3779B97F4A7C15
+
+
+def _splitmix64(state: int) -> tuple[int, int]:
+    state = (state + _GOLDEN) & _M64
+    z = state
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+    return state, z ^ (z >> 31)
+
+
+def _mix64_array(s: np.ndarray) -> np.ndarray:
+    z = s + np.uint64(_GOLDEN)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def device_terrain(nx: int, nz: int, seed: int = 0, octaves: int = 0, base_freq: float = 1.0 / 64.0,
+                   lacunarity: float = 2.0, persistence: float = 0.5, top: float = 0.5, sediment: float = 0.0,
+                   sediment_jitter: float = 0.0, pyramids=()) -> np.ndarray:
+    """Host restatement of swe_world_terrain (float32 [nx, nz])."""
+    f32 = lambda v: float(np.float32(v))  # the C struct holds floats
+    st = seed & _M64
+    p = list(range(256))
+    for k in range(255, 0, -1):
+        st, r = _splitmix64(st)
+        j = r % (k + 1)
+        p[k], p[j] = p[j], p[k]
+    perm = np.array(p + p, dtype=np.int64)
+    st, r = _splitmix64(st)
+    offx = 256.0 * ((r >> 11) * (1.0 / 9007199254740992.0))
+    st, r = _splitmix64(st)
+    offz = 256.0 * ((r >> 11) * (1.0 / 9007199254740992.0))
+    st, jitter_seed = _splitmix64(st)
+    xs = np.arange(nx, dtype=np.float64)[:, None]
+    zs = np.arange(nz, dtype=np.float64)[None, :]
+    if octaves == 0:
+        # map::init's bump in float (cellpool.h:380-385), exp in double
+        px = (np.arange(nx, dtype=np.float32) / np.float32(nx))[:, None]
+        pz = (np.arange(nz, dtype=np.float32) / np.float32(nz))[None, :]
+        dx = (px - np.float32((nx // 4) / np.float32(nx))).astype(np.float32)
+        dz = (pz - np.float32((nz // 2) / np.float32(nz))).astype(np.float32)
+        d = np.sqrt((dx * dx + dz * dz).astype(np.float32)).astype(np.float32)
+        t = ((-d * d).astype(np.float32) * np.float32(nx)).astype(np.float32)
+        v = np.exp(t.astype(np.float64) * 0.2).astype(np.float32)
+        lo, hi = np.float32(min(0.0, float(v.min()))), np.float32(max(0.0, float(v.max())))
+        h = f32(top) * ((v - lo) / (hi - lo)).astype(np.float32).astype(np.float64)
+    else:
+        v = np.zeros((nx, nz), dtype=np.float64)
+        amp, fr = 1.0, f32(base_freq)
+        for _ in range(octaves):
+            v = v + amp * perlin2(xs * fr + offx, zs * fr + offz, perm)
+            amp *= f32(persistence)
+            fr *= f32(lacunarity)
+        lo, hi = float(v.min()), float(v.max())
+        h = (v - lo) / (hi - lo) * f32(top) if hi > lo else np.zeros_like(v)
+    for cx, cz, ph, base in pyramids:
+        d = np.maximum(np.abs(xs - f32(cx)), np.abs(zs - f32(cz))) / (f32(base) / 2.0)
+        h = h + f32(ph) * np.maximum(1.0 - d, 0.0)
+    if sediment != 0.0 or sediment_jitter != 0.0:
+        idx = np.arange(nx * nz, dtype=np.uint64).reshape(nx, nz)
+        with np.errstate(over="ignore"):
+            r = _mix64_array(np.uint64(jitter_seed) + idx * np.uint64(_GOLDEN))
+        u = (r >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+        h = h + (f32(sediment) + f32(sediment_jitter) * (2.0 * u - 1.0))
+    return h.astype(np.float32)

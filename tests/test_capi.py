@@ -76,3 +76,10 @@ def test_null_handles_are_rejected(lib_built):
 def test_wind_direction_is_glm_normalize():
     x, y, z = swe.wind_direction(1, 0, 1)
     assert (x, y, z) == (0.70710677, 0.0, 0.70710677) or abs(x - 0.70710677) < 1e-7
+
+
+def test_batch_rejects_bad_arguments(lib_built):
+    L = swe.lib
+    assert L.swe_batch_erode(None, -1, 1, None) == -1
+    assert L.swe_batch_erode(None, 2, 1, None) == -1
+    assert L.swe_batch_erode(None, 0, 1, None) == 0
