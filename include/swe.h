@@ -267,7 +267,7 @@ int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host
  * parallel erode cycles of `particles_per_cycle` particles (same results as a
  * world whose random-number cycle counter is `first_cycle`), enqueued on
  * `stream` (NULL: the default stream). The scratch it needs lives in one
- * static device array, about 15.5 MB on every GPU that loads the library,
+ * static device array, about 21.5 MB on every GPU that loads the library,
  * held until the process exits; its limits are SWE_NOALLOC_MAX_CELLS cells
  * and SWE_NOALLOC_MAX_PARTICLES particles per cycle, and larger requests fail
  * with SWE_ERR_INVALID. The first call on a device looks up that array's

@@ -96,7 +96,7 @@ struct swe_world {
   int32_t* tape = nullptr;
   long long tape_len = 0;
   // parallel mode
-  int32_t* hq = nullptr;      // heights, exchange deltas, visit counts, cell stamps (4 padded maps)
+  int32_t* hq = nullptr;      // heights, then deltas, visit counts and stamps of even and odd steps (7 padded maps)
   long long* tq = nullptr;    // 4n
   unsigned long long* hw = nullptr;  // n height words of the cluster form
   void* pstate = nullptr;     // 2 buffers x 9 arrays x capacity
@@ -138,12 +138,12 @@ int use_device(swe_world* w) {
 
 // Parallel-mode buffers, grown to hold `particles` in flight.
 int ensure_parallel(swe_world* w, int particles) {
-  // heights, exchange deltas, visit counts and cell stamps, each padded to
-  // 64 elements so every map starts 256-byte aligned.
+  // heights, then exchange deltas, visit counts and cell stamps of even and
+  // odd steps, each padded to 64 elements so every map starts 256-byte aligned.
   const size_t stride = ((size_t)w->n + 63) & ~(size_t)63;
   if (!w->hq) {
-    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 4 * stride));
-    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 4 * stride, w->stream));
+    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 7 * stride));
+    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 7 * stride, w->stream));
     SWE_CK(cudaMalloc(&w->tq, sizeof(long long) * 4 * w->n));
     SWE_CK(cudaMalloc(&w->hw, sizeof(unsigned long long) * w->n));
     SWE_CK(cudaMemsetAsync(w->tq, 0, sizeof(long long) * 4 * w->n, w->stream));
@@ -165,6 +165,9 @@ int ensure_parallel(swe_world* w, int particles) {
   B.dq = w->hq + stride;
   B.visits = w->hq + 2 * stride;
   B.stamp = reinterpret_cast<uint32_t*>(w->hq + 3 * stride);
+  B.dq2 = w->hq + 4 * stride;
+  B.visits2 = w->hq + 5 * stride;
+  B.stamp2 = reinterpret_cast<uint32_t*>(w->hq + 6 * stride);
   B.hw = w->hw;
   for (int k = 0; k < 4; k++) B.tq[k] = w->tq + (size_t)k * w->n;
   int32_t* base = reinterpret_cast<int32_t*>(w->pstate);

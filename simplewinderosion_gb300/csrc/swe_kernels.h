@@ -36,8 +36,14 @@ struct ParallelBuffers {
   int32_t* hq;         // fixed-point heights
   int32_t* dq;         // exchange deltas pending for the cascade passes (zero between steps)
   int32_t* visits;     // cascades owed per cell (zero between steps)
-  uint32_t* stamp;     // cluster form: per cell, the step (from 1) in which it was last visited
-  unsigned long long* hw;  // cluster form: height words (fixed-point height, write tag)
+  // bounded-lanes form: the maps of odd steps (the even steps use dq, visits
+  // and stamp), so that a step's flights can start while the previous step's
+  // last cascades finish
+  int32_t* dq2;
+  int32_t* visits2;
+  uint32_t* stamp;     // per cell, the step (from 1) in which it was last visited (even steps)
+  uint32_t* stamp2;    // the same for odd steps
+  unsigned long long* hw;  // height words (fixed-point height, write tag)
   long long* tq[4];    // track accumulators (massflow, momx, momy, momz), 2^-32 units
   ParticleSoA state[2];
   int capacity;        // particles the state buffers hold

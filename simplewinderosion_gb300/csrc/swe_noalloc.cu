@@ -27,7 +27,7 @@ constexpr size_t kMaxCells = SWE_NOALLOC_MAX_CELLS;          // a multiple of 64
 constexpr size_t kMaxParticles = SWE_NOALLOC_MAX_PARTICLES;
 constexpr size_t kCountersBytes = align256(sizeof(swe::Counters));
 constexpr size_t kBarrierBytes = align256(sizeof(swe::GridBarrier));
-constexpr size_t kMapsBytes = 4 * kMaxCells * sizeof(int32_t);      // heights, deltas, owed cascades, stamps
+constexpr size_t kMapsBytes = 7 * kMaxCells * sizeof(int32_t);  // heights; deltas, owed cascades, stamps x2
 constexpr size_t kTracksBytes = 4 * kMaxCells * sizeof(long long);   // track accumulators
 constexpr size_t kWordsBytes = kMaxCells * sizeof(unsigned long long);  // height words
 constexpr size_t kParticleBytes = 2 * 9 * kMaxParticles * sizeof(int32_t);  // two state buffers
@@ -123,6 +123,9 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   B.dq = maps + stride;
   B.visits = maps + 2 * stride;
   B.stamp = reinterpret_cast<uint32_t*>(maps + 3 * stride);
+  B.dq2 = maps + 4 * stride;
+  B.visits2 = maps + 5 * stride;
+  B.stamp2 = reinterpret_cast<uint32_t*>(maps + 6 * stride);
   B.hw = words;
   for (int k = 0; k < 4; k++) B.tq[k] = tracks + (size_t)k * n;
   for (int b = 0; b < 2; b++) {
@@ -166,6 +169,7 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   SWE_NA_CK(cudaMemsetAsync(cnt, 0, sizeof(swe::Counters), s));
   SWE_NA_CK(cudaMemcpyAsync(&cnt->cycle, &first_cycle, sizeof(first_cycle), cudaMemcpyHostToDevice, s));
   SWE_NA_CK(cudaMemsetAsync(B.dq, 0, 2 * stride * sizeof(int32_t), s));
+  SWE_NA_CK(cudaMemsetAsync(B.dq2, 0, 2 * stride * sizeof(int32_t), s));
   swe::launch_height_to_fixed(F.f[0], B.hq, c, cnt, s);
   SWE_NA_CK(cudaGetLastError());
   for (int k = 0; k < cycles; k++) {

@@ -142,20 +142,52 @@ __device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
   return s_ok != 0;
 }
 
-// The same barrier with one arrival counter, for grids of one block per SM:
-// a single atomic per block, the last arrival releases the generation.
-__device__ bool grid_sync_flat(GridBarrier* gb, unsigned int* status) {
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long atom_add_acq_rel64(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ void st_release64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void st_relaxed64u(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// The flat barrier whose arrivals also add up one count per block: *below
+// gets the sum over the blocks that arrived before this one, *total the sum
+// over all blocks (the arrival order stands in for a block order).
+__device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned mine, unsigned* below,
+                              unsigned* total) {
   __shared__ int s_ok;
+  __shared__ unsigned s_below, s_total;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned g = ld_acquire(&gb->gen);
-    if (atom_add_acq_rel(&gb->count, 1u) == gridDim.x - 1) {
-      st_relaxed(&gb->count, 0u);
-      atom_add_release(&gb->gen, 1u);
+    const unsigned g = (unsigned)(ld_acquire64(&gb->gen64) >> 32);
+    const unsigned long long old = atom_add_acq_rel64(&gb->count64, (1ull << 32) | mine);
+    const unsigned b = (unsigned)old;
+    unsigned tot = 0;
+    if ((unsigned)(old >> 32) == gridDim.x - 1) {
+      tot = b + mine;
+      st_relaxed64u(&gb->count64, 0ull);
+      st_release64(&gb->gen64, ((unsigned long long)(g + 1u) << 32) | tot);
     } else {
       const unsigned long long t0 = global_ns();
-      while (ld_acquire(&gb->gen) == g) {
+      for (;;) {
+        const unsigned long long w = ld_acquire64(&gb->gen64);
+        if ((unsigned)(w >> 32) != g) {
+          tot = (unsigned)w;
+          break;
+        }
         if (ld_acquire(&gb->abort)) {
           ok = 0;
           break;
@@ -169,9 +201,13 @@ __device__ bool grid_sync_flat(GridBarrier* gb, unsigned int* status) {
       }
     }
     if (ld_acquire(&gb->abort)) ok = 0;
+    s_below = b;
+    s_total = tot;
     s_ok = ok;
   }
   __syncthreads();
+  *below = s_below;
+  *total = s_total;
   return s_ok != 0;
 }
 
@@ -263,40 +299,31 @@ struct Particle {
   float px, py, pz, vx, vy, vz;
 };
 
-// Heights read by the fly step: an int32 map through L1 in the grid kernel;
-// in the cluster kernel the low halves of the 64-bit height words, from L2
-// (its cascades write the map from other SMs between steps).
-template <bool kWords>
-__device__ __forceinline__ int32_t load_h(const int32_t* H, long i) {
-  if constexpr (kWords) return __ldcg(H + 2 * i);
-  else return H[i];
+// The cell a particle is over (its position rounded, as ivec2(round(...)),
+// wind.hpp:30), or -1 off the map.
+__device__ __forceinline__ long particle_cell(const Consts& c, const Particle& p, int& ix, int& iz) {
+  const bool inrange = fabsf(p.px) < 1073741824.0f && fabsf(p.pz) < 1073741824.0f;
+  ix = inrange ? (int)roundf(p.px) : -1;
+  iz = inrange ? (int)roundf(p.pz) : -1;
+  if (ix < 0 || iz < 0 || ix >= c.nx || iz >= c.nz) return -1;
+  return (long)ix * c.nz + iz;
 }
 
-// One Wind::fly step (wind.hpp:28-117) of particle p against the heights H
-// as they were at the start of the step. A survivor adds its tracks
-// (wind.hpp:93-96) and its exchange with the cell (wind.hpp:110-112) to the
-// accumulators, moves, and the index of the cell it flew from is returned;
-// the caller records the cascade it owes that cell (wind.hpp:114). A particle
-// that dies returns -1 and writes nothing (its sediment is exported).
-template <bool kWords>
-__device__ __forceinline__ long fly_particle(const Consts& c, const ParallelBuffers& B, const int32_t* H, uint32_t c_lo,
-                                             uint32_t c_hi, uint32_t seed_lo, uint32_t seed_hi, Particle& p,
-                                             unsigned& status) {
+// One Wind::fly step (wind.hpp:28-117) of particle p over cell ci = (ix, iz),
+// given the step-start heights of the cell and of its x-1, x+1, z-1, z+1
+// neighbours (fixed point; those off the map are not used). A survivor adds
+// its tracks (wind.hpp:93-96) and its exchange with the cell
+// (wind.hpp:110-112) to the accumulators (exchange into dq), moves, and ci is
+// returned; the caller records the cascade it owes the cell (wind.hpp:114). A
+// particle that dies returns -1 and writes nothing (its sediment is exported).
+__device__ __forceinline__ long fly_from(const Consts& c, const ParallelBuffers& B, int32_t* dq, long ci, int ix,
+                                         int iz, int32_t q11, int32_t q01, int32_t q21, int32_t q10, int32_t q12,
+                                         uint32_t c_lo, uint32_t c_hi, uint32_t seed_lo, uint32_t seed_hi,
+                                         Particle& p, unsigned& status) {
   const int nx = c.nx, nz = c.nz;
   const float inv = c.inv_scale;
   const float sed = fx2f(p.sed_q, inv);
-  const bool inrange = fabsf(p.px) < 1073741824.0f && fabsf(p.pz) < 1073741824.0f;
-  const int ix = inrange ? (int)roundf(p.px) : -1;
-  const int iz = inrange ? (int)roundf(p.pz) : -1;
-  if (ix < 0 || iz < 0 || ix >= nx || iz >= nz) return -1;
   const bool vx0 = ix > 0, vx2 = ix + 1 < nx, vz0 = iz > 0, vz2 = iz + 1 < nz;
-  const long ci = (long)ix * nz + iz;
-  // five unconditional loads (a missing neighbour reads the cell itself)
-  const int32_t q11 = load_h<kWords>(H, ci);
-  const int32_t q01 = load_h<kWords>(H, vx0 ? ci - nz : ci);
-  const int32_t q21 = load_h<kWords>(H, vx2 ? ci + nz : ci);
-  const int32_t q10 = load_h<kWords>(H, vz0 ? ci - 1 : ci);
-  const int32_t q12 = load_h<kWords>(H, vz2 ? ci + 1 : ci);
   const float h11 = fx2f(q11, inv);
   const float h01 = vx0 ? fx2f(q01, inv) : 0.0f;
   const float h21 = vx2 ? fx2f(q21, inv) : 0.0f;
@@ -352,11 +379,28 @@ __device__ __forceinline__ long fly_particle(const Consts& c, const ParallelBuff
   atomicAdd((unsigned long long*)&B.tq[3][ci], (unsigned long long)to_fixed64(sp.z * kTwo32));
   // Exchange with the cell (wind.hpp:110-112), in fixed point.
   const int32_t ex_q = to_fixed(c.suspension * diff * c.scale);
-  atomicAdd(B.dq + ci, -ex_q);
+  atomicAdd(dq + ci, -ex_q);
   p.sed_q = wrap_add(p.sed_q, ex_q);
   p.px = npx; p.py = npy; p.pz = npz;
   p.vx = sp.x; p.vy = sp.y; p.vz = sp.z;
   return ci;
+}
+
+// The whole step, reading the heights from the int32 map H.
+__device__ __forceinline__ long fly_particle(const Consts& c, const ParallelBuffers& B, const int32_t* H,
+                                             uint32_t c_lo, uint32_t c_hi, uint32_t seed_lo, uint32_t seed_hi,
+                                             Particle& p, unsigned& status) {
+  int ix, iz;
+  const long ci = particle_cell(c, p, ix, iz);
+  if (ci < 0) return -1;
+  const int nz = c.nz;
+  // five unconditional loads (a missing neighbour reads the cell itself)
+  const int32_t q11 = H[ci];
+  const int32_t q01 = H[ix > 0 ? ci - nz : ci];
+  const int32_t q21 = H[ix + 1 < c.nx ? ci + nz : ci];
+  const int32_t q10 = H[iz > 0 ? ci - 1 : ci];
+  const int32_t q12 = H[iz + 1 < nz ? ci + 1 : ci];
+  return fly_from(c, B, B.dq, ci, ix, iz, q11, q01, q21, q10, q12, c_lo, c_hi, seed_lo, seed_hi, p, status);
 }
 
 // Fly phase of one step: Wind::fly for every particle in flight against the
@@ -381,7 +425,7 @@ __device__ void fly_phase(const CycleArgs& A, int in, int count, uint32_t c_lo, 
       p.id = S.id[i]; p.age = S.age[i]; p.sed_q = S.sed_q[i];
       p.px = S.px[i]; p.py = S.py[i]; p.pz = S.pz[i];
       p.vx = S.vx[i]; p.vy = S.vy[i]; p.vz = S.vz[i];
-      const long ci = fly_particle<false>(A.c, A.B, A.B.hq, c_lo, c_hi, A.seed_lo, A.seed_hi, p, status);
+      const long ci = fly_particle(A.c, A.B, A.B.hq, c_lo, c_hi, A.seed_lo, A.seed_hi, p, status);
       if (ci >= 0) {
         atomicAdd(A.B.visits + ci, 1);  // one cascade owed to the cell (wind.hpp:114)
         alive = true;
@@ -762,6 +806,7 @@ __device__ void prologue_cells(const ParallelBuffers& B, long n, long i0, long s
   for (long i = i0; i < n; i += stride) {
     B.hw[i] = (unsigned long long)(uint32_t)B.hq[i];
     B.stamp[i] = 0;
+    B.stamp2[i] = 0;
     B.tq[0][i] = 0; B.tq[1][i] = 0; B.tq[2][i] = 0; B.tq[3][i] = 0;
   }
 }
@@ -966,10 +1011,9 @@ __host__ __device__ constexpr unsigned near_mask(int qu, int qw) {
 // (grid barriers, lane counts in global memory).
 template <bool kCluster>
 __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32_t* dyn) {
-  __shared__ int s_free;               // free lanes of this CTA, read by the other CTAs
+  __shared__ int s_free[2];            // free lanes of this CTA by step parity, read by the other CTAs
   __shared__ int s_all[kClusterCtas];  // every CTA's free lanes, this step
   __shared__ int s_warp[32];
-  __shared__ int s_sum[2][32];
   __shared__ unsigned long long s_time[3];  // fly, cascades, last mark (CTA 0's thread 0)
   const int T = blockDim.x;
   const int cap = slots * T;
@@ -978,7 +1022,21 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   auto PF = [&](int f, int j) -> float& { return reinterpret_cast<float*>(dyn)[f * cap + j]; };
   int* s_own = dyn + 9 * cap;        // per lane slot: the cell it owns this step
   int* s_vis = dyn + 10 * cap;       // per lane slot: cascades the owned cell owes
-  int32_t* N = dyn + 11 * cap + 9 * threadIdx.x;  // this thread's 3x3 neighbourhood
+  int* s_ox = dyn + 11 * cap;        // per lane slot: the owned cell's x
+  int32_t* N = dyn + 12 * cap + 9 * threadIdx.x;  // this thread's 3x3 neighbourhood
+  // Per cell colour (x%3, z%3): the cells of the 5x5 block around (bit
+  // (du+2)*5 + dw+2) whose colour is lower.
+  __shared__ unsigned s_lower[9];
+  if (threadIdx.x < 9) {
+    const int xr = threadIdx.x / 3, zr = threadIdx.x % 3;
+    unsigned m = 0;
+    for (int k = 0; k < 25; k++) {
+      const int du = k / 5 - 2, dw = k % 5 - 2;
+      if (((xr + du + 3) % 3) * 3 + (zr + dw + 3) % 3 < xr * 3 + zr) m |= 1u << k;
+    }
+    s_lower[threadIdx.x] = m;
+  }
+  __syncthreads();
 
   const Consts& c = A.c;
   const ParallelBuffers& B = A.B;
@@ -1015,101 +1073,21 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   unsigned steps = 0;
   unsigned status = 0;
   bool gave_up = false;
-  int nid = 0;  // next particle id of the cycle
   // Every step advances a particle, and each flies at most max_age + 2 steps:
   // a bound that is never reached (past it the cycle stops with
   // SWE_STATUS_TIMEOUT).
   const unsigned long long bound = (unsigned long long)A.particles * (c.max_age + 2) + 2;
   const unsigned max_steps = bound > kClusterMaxSteps ? kClusterMaxSteps : (unsigned)bound;
-  unsigned step = 0;
-  for (;; step++) {
-    if (cst.transfers > 0x40000000u || cst.cascades > 0x40000000u || steps > 0x40000000u) {
-      atomicAdd(&cnt->transfers, (unsigned long long)cst.transfers);
-      atomicAdd(&cnt->cascades, (unsigned long long)cst.cascades);
-      atomicAdd(&cnt->particle_steps, (unsigned long long)steps);
-      cst.transfers = 0;
-      cst.cascades = 0;
-      steps = 0;
-    }
-    // Free lanes of this thread and their rank within the CTA.
-    const unsigned freem = lanes_mask & ~live;
-    const int f = __popc(freem);
-    int incl = f;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    int wpre = 0, btotal = 0;
-    for (int k = 0; k < nwarps; k++) {
-      const int v = s_warp[k];
-      wpre += k < warp ? v : 0;
-      btotal += v;
-    }
-    int total_free = 0, base = 0;
-    if constexpr (kCluster) {
-      if (t == 0) s_free = btotal;
-      cluster_barrier();  // B1: the last step's cascades are done everywhere
-      ph++;
-      if (timer) {
-        const unsigned long long now = global_ns();
-        s_time[1] += now - s_time[2];
-        s_time[2] = now;
-      }
-      if (aborted_before(A.gb, ph)) break;
-      if (t < kClusterCtas) s_all[t] = ld_dsmem(&s_free, (unsigned)t);
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < kClusterCtas; k++) {
-        const int v = s_all[k];
-        total_free += v;
-        base += k < (int)r ? v : 0;
-      }
-    } else {
-      if (t == 0) A.gb->lanes_free[r] = btotal;
-      if (!grid_sync_flat(A.gb, &cnt->status)) break;  // B1
-      ph++;
-      if (timer) {
-        const unsigned long long now = global_ns();
-        s_time[1] += now - s_time[2];
-        s_time[2] = now;
-      }
-      int tot = 0, below = 0;
-      for (int k = t; k < nb; k += T) {
-        const int v = __ldcg(&A.gb->lanes_free[k]);
-        tot += v;
-        below += k < (int)r ? v : 0;
-      }
-      tot = warp_sum(tot);
-      below = warp_sum(below);
-      if (lane == 0) {
-        s_sum[0][warp] = tot;
-        s_sum[1][warp] = below;
-      }
-      __syncthreads();
-      for (int k = 0; k < nwarps; k++) {
-        total_free += s_sum[0][k];
-        base += s_sum[1][k];
-      }
-    }
-    const int survivors = L - total_free;
-    int refill = A.particles - nid;
-    if (refill > total_free) refill = total_free;
-    if (survivors == 0 && refill == 0) break;
-    if (step >= max_steps) {
-      status |= 0x8u;  // SWE_STATUS_TIMEOUT
-      break;
-    }
 
-    // The cycle's next particles take the free lanes (ids nid .. nid+refill-1).
-    int rank = base + wpre + (incl - f);
+  // The cycle's particles with ids from `first` take the free lanes `freem`
+  // of this thread; `rank` is the CTA-wide rank of its first free lane among
+  // all free lanes, and `count` lanes in all are filled.
+  auto spawn = [&](unsigned freem, int rank, int first, int count) {
 #pragma unroll
     for (int s = 0; s < kClusterMaxSlots; s++) {
       if ((freem >> s) & 1u) {
-        if (rank < refill) {
-          const int id = nid + rank;
+        if (rank < count) {
+          const int id = first + rank;
           const uint4 u = philox4x32((uint32_t)id, 0xFFFFFFFFu, c_lo, c_hi, A.seed_lo, A.seed_hi);
           const int j = s * T + t;
           PI(0, j) = id;
@@ -1124,27 +1102,148 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         rank++;
       }
     }
-    nid += refill;
+  };
+  // CTA-wide exclusive prefix of the threads' counts f (and the CTA total).
+  auto block_scan = [&](int f, int* total) -> int {
+    int incl = f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    __syncthreads();  // s_warp is free again
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int wpre = 0, tot = 0;
+    for (int k = 0; k < nwarps; k++) {
+      const int v = s_warp[k];
+      wpre += k < warp ? v : 0;
+      tot += v;
+    }
+    *total = tot;
+    return wpre + incl - f;
+  };
 
-    // Fly.
+  // The first lanes of the cycle: every lane free, ids in lane order.
+  int nid;
+  {
+    int btotal = 0;
+    const int pre = block_scan(__popc(lanes_mask), &btotal);
+    const int base0 = (int)r * (L / nb) + ((int)r < L % nb ? (int)r : L % nb);
+    nid = A.particles < L ? A.particles : L;
+    spawn(lanes_mask, base0 + pre, 0, nid);
+  }
+
+  // One step: every particle flies once its five cells have had every write
+  // of the previous step (the tags of their words say so); one barrier, at
+  // which the free lanes are counted; the next particles take the free lanes;
+  // the owned cells absorb their deltas and run their cascades. A thread goes
+  // on to its next flight as soon as its own cascades are done: the deltas,
+  // visit counts and stamps of consecutive steps live in separate maps.
+  for (unsigned step = 0;; step++) {
+    if (cst.transfers > 0x40000000u || cst.cascades > 0x40000000u || steps > 0x40000000u) {
+      atomicAdd(&cnt->transfers, (unsigned long long)cst.transfers);
+      atomicAdd(&cnt->cascades, (unsigned long long)cst.cascades);
+      atomicAdd(&cnt->particle_steps, (unsigned long long)steps);
+      cst.transfers = 0;
+      cst.cascades = 0;
+      steps = 0;
+    }
+    const unsigned odd = step & 1u;
     const unsigned vmark = step + 1;     // visited stamp of this step
     const unsigned tbase = 16u * vmark;  // tag base of this step
-    unsigned owned = 0;                  // bit s: slot s owns its cell this step
+    uint32_t* stamp = odd ? B.stamp2 : B.stamp;
+    const uint32_t* stamp_prev = odd ? B.stamp : B.stamp2;
+    int32_t* visits = odd ? B.visits2 : B.visits;
+    int32_t* dq = odd ? B.dq2 : B.dq;
+
+    // Fly.
+    unsigned owned = 0;  // bit s: slot s owns its cell this step
 #pragma unroll
     for (int s = 0; s < kClusterMaxSlots; s++) {
+      if (s >= slots) break;
+      const int j = s * T + t;
+      Particle p;
+      long ci = -1;
+      int ix = 0, iz = 0;
       if ((live >> s) & 1u) {
-        const int j = s * T + t;
-        Particle p;
         p.id = PI(0, j); p.age = PI(1, j); p.sed_q = PI(2, j);
         p.px = PF(3, j); p.py = PF(4, j); p.pz = PF(5, j);
         p.vx = PF(6, j); p.vy = PF(7, j); p.vz = PF(8, j);
-        const long ci = fly_particle<true>(c, B, reinterpret_cast<const int32_t*>(HW), c_lo, c_hi, A.seed_lo,
-                                           A.seed_hi, p, status);
+        ci = particle_cell(c, p, ix, iz);
+      }
+      // The five cells' words (bits 0..4: the cell, x-1, x+1, z-1, z+1),
+      // each read until its tag shows every write of the previous step: the
+      // cell's delta if it was visited, and the cascades of the visited cells
+      // next to it (from the previous step's stamps of the 5x5 block).
+      const long nbr[5] = {0, -(long)nz, (long)nz, -1, 1};
+      const int qpos[5] = {12, 7, 17, 11, 13};  // positions in the 5x5 block
+      unsigned need = 0, ready = 0, prev = 0;
+      int32_t hv[5] = {0, 0, 0, 0, 0};
+      if (ci >= 0) {
+        need = 1u | (ix > 0 ? 2u : 0u) | (ix + 1 < nx ? 4u : 0u) | (iz > 0 ? 8u : 0u) | (iz + 1 < nz ? 16u : 0u);
+        if (step > 0) {
+          unsigned rows = 0, cols = 0;
+#pragma unroll
+          for (int d = -2; d <= 2; d++) {
+            rows |= (ix + d >= 0 && ix + d < nx) ? 1u << (d + 2) : 0u;
+            cols |= (iz + d >= 0 && iz + d < nz) ? 1u << (d + 2) : 0u;
+          }
+          unsigned inm = 0;
+#pragma unroll
+          for (int d = 0; d < 5; d++) inm |= ((rows >> d) & 1u) ? cols << (5 * d) : 0u;
+          unsigned sv[25];
+#pragma unroll
+          for (int k = 0; k < 25; k++)
+            sv[k] = __ldcg(stamp_prev + (((inm >> k) & 1u) ? ci + (k / 5 - 2) * nz + (k % 5 - 2) : ci));
+#pragma unroll
+          for (int k = 0; k < 25; k++) prev |= sv[k] == step ? 1u << k : 0u;
+          prev &= inm;
+        }
+      }
+      const unsigned pbase = 16u * step;  // tag base of the previous step
+      unsigned long long t_wait = 0;
+      for (;;) {
+        unsigned long long wd[5];
+#pragma unroll
+        for (int q = 0; q < 5; q++)
+          wd[q] = (((need & ~ready) >> q) & 1u) ? ld_relaxed64(HW + ci + nbr[q]) : 0ull;
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          if (((need & ~ready) >> q) & 1u) {
+            const int qu = qpos[q] / 5 - 2, qw = qpos[q] % 5 - 2;
+            const unsigned want = step ? __popc(prev & near_mask(qu, qw)) + ((prev >> qpos[q]) & 1u) : 0u;
+            if (step == 0 || tag_ready(word_tag(wd[q]), pbase, want)) {
+              hv[q] = word_height(wd[q]);
+              ready |= 1u << q;
+            }
+          }
+        }
+        if (ready != need && !gave_up) {
+          const unsigned long long now = global_ns();
+          if (t_wait == 0) t_wait = now;
+          if (now - t_wait > kBarrierLimitNs || ld_volatile(reinterpret_cast<const int*>(&A.gb->abort)) != 0) {
+            status |= 0x8u;  // SWE_STATUS_TIMEOUT
+            atomicCAS(&A.gb->abort, 0u, ph + 1);
+            gave_up = true;
+          }
+        }
+        if (gave_up) ready = need;
+        if (!__any_sync(0xffffffffu, ready != need)) break;
+        __nanosleep(64);
+      }
+      if ((live >> s) & 1u) {
+        if (ci >= 0 && !gave_up)
+          ci = fly_from(c, B, dq, ci, ix, iz, hv[0], hv[1], hv[2], hv[3], hv[4], c_lo, c_hi, A.seed_lo, A.seed_hi,
+                        p, status);
+        else
+          ci = -1;
         if (ci >= 0) {
           steps++;
-          if (atomicAdd(B.visits + ci, 1) == 0) {
-            __stcg(B.stamp + ci, vmark);
+          if (atomicAdd(visits + ci, 1) == 0) {
+            __stcg(stamp + ci, vmark);
             s_own[j] = (int)ci;
+            s_ox[j] = ix;
             owned |= 1u << s;
           }
           PI(1, j) = p.age; PI(2, j) = p.sed_q;
@@ -1156,18 +1255,47 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         }
       }
     }
+
+    // The step's one barrier: every exchange and visit of the step is in,
+    // and the free lanes are counted on the way.
+    const unsigned freem = lanes_mask & ~live;
+    int btotal = 0;
+    const int pre = block_scan(__popc(freem), &btotal);
+    int total_free = 0, base = 0;
     if constexpr (kCluster) {
-      cluster_barrier();  // B2: every exchange and visit of the step is in
+      if (t == 0) s_free[odd] = btotal;
+      cluster_barrier();
       ph++;
       if (aborted_before(A.gb, ph)) break;
+      if (t < kClusterCtas) s_all[t] = ld_dsmem(&s_free[odd], (unsigned)t);
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kClusterCtas; k++) {
+        const int v = s_all[k];
+        total_free += v;
+        base += k < (int)r ? v : 0;
+      }
     } else {
-      if (!grid_sync_flat(A.gb, &cnt->status)) break;  // B2
+      unsigned below = 0, tot = 0;
+      if (!grid_sync_sum(A.gb, &cnt->status, (unsigned)btotal, &below, &tot)) break;
       ph++;
+      total_free = (int)tot;
+      base = (int)below;
     }
     if (timer) {
       const unsigned long long now = global_ns();
       s_time[0] += now - s_time[2];
       s_time[2] = now;
+    }
+    const int survivors = L - total_free;
+    int refill = A.particles - nid;
+    if (refill > total_free) refill = total_free;
+    // Nobody flew (no survivors, so no writes) and nobody is left: done.
+    const bool done = (survivors == 0 && refill == 0) || step + 1 >= max_steps;
+    if (step + 1 >= max_steps && !(survivors == 0 && refill == 0)) status |= 0x8u;  // SWE_STATUS_TIMEOUT
+    if (!done) {
+      spawn(freem, base + pre, nid, refill);
+      nid += refill;
     }
 
     // The owned cells' deltas: the first write of each in the step.
@@ -1175,12 +1303,12 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
     for (int s = 0; s < kClusterMaxSlots; s++) {
       if ((owned >> s) & 1u) {
         const int ci = s_own[s * T + t];
-        const int v = __ldcg(B.visits + ci);
-        const int32_t d = __ldcg(B.dq + ci);
+        const int v = __ldcg(visits + ci);
+        const int32_t d = __ldcg(dq + ci);
         const unsigned long long w = ld_relaxed64(HW + ci);
         s_vis[s * T + t] = v;
-        __stcg(B.visits + ci, 0);
-        __stcg(B.dq + ci, 0);
+        __stcg(visits + ci, 0);
+        __stcg(dq + ci, 0);
         st_relaxed64(HW + ci, make_word(wrap_add(word_height(w), d), tbase + 1));
       }
     }
@@ -1194,7 +1322,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       unsigned todo = owned;  // slots whose cell still owes its cascades
       int cs = -1;            // slot of the cell in hand
       int ci = 0, x = 0, z = 0;
-      unsigned visited = 0, lower = 0, ready = 0, okmask = 0;
+      unsigned visited = 0, lower = 0, ready = 0, okmask = 0, inmask = 0;
       unsigned long long t_wait = 0;
       for (;;) {
         bool progressed = false;
@@ -1202,37 +1330,48 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         unsigned sv[25];
         if (cs < 0 && todo && !gave_up) {
           // the lowest-colour cell left
-          int best = 9;
+          if (slots == 1) {
+            cs = 0;
+          } else {
+            int best = 9;
 #pragma unroll
-          for (int s2 = 0; s2 < kClusterMaxSlots; s2++) {
-            if ((todo >> s2) & 1u) {
-              const int c2 = s_own[s2 * T + t];
-              const int x2 = c2 / nz, z2 = c2 - x2 * nz;
-              const int col2 = (x2 % 3) * 3 + z2 % 3;
-              if (col2 < best) {
-                best = col2;
-                cs = s2;
+            for (int s2 = 0; s2 < kClusterMaxSlots; s2++) {
+              if ((todo >> s2) & 1u) {
+                const int x2 = s_ox[s2 * T + t], z2 = s_own[s2 * T + t] - x2 * nz;
+                const int col2 = (x2 % 3) * 3 + z2 % 3;
+                if (col2 < best) {
+                  best = col2;
+                  cs = s2;
+                }
               }
             }
           }
           ci = s_own[cs * T + t];
-          x = ci / nz;
+          x = s_ox[cs * T + t];
           z = ci - x * nz;
+          // In-map rows and columns of the 5x5 block, as bit masks.
+          unsigned rows = 0, cols = 0;
+#pragma unroll
+          for (int d = -2; d <= 2; d++) {
+            rows |= (x + d >= 0 && x + d < nx) ? 1u << (d + 2) : 0u;
+            cols |= (z + d >= 0 && z + d < nz) ? 1u << (d + 2) : 0u;
+          }
+          inmask = 0;
+#pragma unroll
+          for (int d = 0; d < 5; d++) inmask |= ((rows >> d) & 1u) ? cols << (5 * d) : 0u;
           // Stamps of the 5x5 block around (cells off the map read the
           // cell's own stamp and are masked below).
 #pragma unroll
           for (int k = 0; k < 25; k++) {
             const int du = k / 5 - 2, dw = k % 5 - 2;
-            const bool in = x + du >= 0 && x + du < nx && z + dw >= 0 && z + dw < nz;
-            sv[k] = __ldcg(B.stamp + (in ? ci + du * nz + dw : ci));
+            sv[k] = __ldcg(stamp + (((inmask >> k) & 1u) ? ci + du * nz + dw : ci));
           }
+          // the 3x3 neighbourhood's in-map cells (bit 3u+w)
           okmask = 0;
 #pragma unroll
           for (int u = 0; u < 3; u++)
 #pragma unroll
-            for (int w = 0; w < 3; w++)
-              if ((u == 0 ? x > 0 : (u == 2 ? x + 1 < nx : true)) && (w == 0 ? z > 0 : (w == 2 ? z + 1 < nz : true)))
-                okmask |= 1u << (3 * u + w);
+            for (int w = 0; w < 3; w++) okmask |= ((inmask >> ((u + 1) * 5 + w + 1)) & 1u) << (3 * u + w);
           ready = 0;
           t_wait = 0;
           fresh = true;
@@ -1248,18 +1387,11 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         }
         if (fresh) {
           // visited cells of the 5x5 block, and those of lower colour
-          const int xr = x % 3, zr = z % 3, col = xr * 3 + zr;
-          visited = 1u << 12;
-          lower = 0;
+          visited = 0;
 #pragma unroll
-          for (int k = 0; k < 25; k++) {
-            const int du = k / 5 - 2, dw = k % 5 - 2;
-            const bool in = x + du >= 0 && x + du < nx && z + dw >= 0 && z + dw < nz;
-            const bool v = k != 12 && in && sv[k] == vmark;
-            const bool lo = ((xr + du + 3) % 3) * 3 + (zr + dw + 3) % 3 < col;
-            visited |= v ? 1u << k : 0u;
-            lower |= (v && lo) ? 1u << k : 0u;
-          }
+          for (int k = 0; k < 25; k++) visited |= sv[k] == vmark ? 1u << k : 0u;
+          visited = (visited & inmask) | (1u << 12);
+          lower = visited & s_lower[(x % 3) * 3 + z % 3];
         }
         if (cs >= 0) {
           // Take the words whose tags show every earlier write (the cell's
@@ -1310,6 +1442,12 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         if (!__any_sync(0xffffffffu, progressed)) __nanosleep(64);
       }
     }
+    if (timer) {
+      const unsigned long long now = global_ns();
+      s_time[1] += now - s_time[2];
+      s_time[2] = now;
+    }
+    if (done) break;
   }
   // No CTA may leave while another can still read its shared memory.
   if constexpr (kCluster) cluster_barrier();
@@ -1472,9 +1610,9 @@ bool lanes_shape(int lanes, int ctas, int max_threads, int* threads, int* slots)
   return true;
 }
 
-// particle state (9 words) and owned cell + owed cascades (2 words) per lane
-// slot, and a 3x3 neighbourhood per thread
-size_t lanes_smem(int threads, int slots) { return sizeof(int32_t) * (size_t)threads * (11 * slots + 9); }
+// particle state (9 words) and owned cell, owed cascades and the cell's x
+// (3 words) per lane slot, and a 3x3 neighbourhood per thread
+size_t lanes_smem(int threads, int slots) { return sizeof(int32_t) * (size_t)threads * (12 * slots + 9); }
 
 cudaError_t launch_cluster(const CycleArgs& A, int threads, int slots, cudaStream_t s, bool* launched) {
   *launched = false;

@@ -62,6 +62,12 @@ struct GridBarrier {
   unsigned int pad[29];
   unsigned int leaf[16 * 32];  // block arrivals per leaf, one 128-byte line each
   int lanes_free[1024];        // bounded-lanes kernel: free lanes per block, this step
+  // A second flat barrier whose arrivals also sum a per-block count:
+  // arrivals << 32 | running sum, and generation << 32 | the step's total.
+  unsigned long long count64;
+  unsigned long long pad64a[15];
+  unsigned long long gen64;
+  unsigned long long pad64b[15];
 };
 
 // Particle state of the parallel mode, structure of arrays.
