@@ -116,6 +116,25 @@ def config_dict(args, particles):
     }
 
 
+# ---------------------------------------------------------------- multi-rank
+def max_over_ranks(x: float, device="cpu") -> float:
+    """The largest of every rank's x (the job's time is its slowest rank's);
+    x itself with one process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world_size: int, total_ms: float) -> float:
+    """Units per second of the whole job: every rank's units over the
+    slowest rank's time (replicas: the map does not shard)."""
+    return units_per_rank * world_size / (total_ms / 1e3)
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clock / throttle samples while the timed region runs."""
@@ -311,13 +330,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     if world_size > 1:
         dist.barrier()
-        tmax = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        total_ms = float(tmax.item())
+    total_ms = max_over_ranks(total_ms, dev)
     clocks = sampler.stop() if sampler else None
 
-    cycles_total = args.steps * world_size
-    value = cycles_total / (total_ms / 1e3)
+    value = whole_job_rate(args.steps, world_size, total_ms)
     ms_per_step = total_ms / args.steps
 
     # Roofline of the dominant kernel. One erode cycle is one launch of the
@@ -362,7 +378,7 @@ def run_ours(args):
         "dtype": "f32+i32",
         "data": "synthetic",
         "config": config_dict(args, particles),
-        "particle_steps_per_s": psteps * world_size / (total_ms / 1e3),
+        "particle_steps_per_s": whole_job_rate(psteps, world_size, total_ms),
         "kernels": {"cycle_ms": ms_per_step, "fly_phases_ms": fly_ms / args.steps,
                     "cascade_phases_ms": cas_ms / args.steps, "k_transfers_per_step": k,
                     "particle_steps_per_cycle": psteps_per_launch},
@@ -428,12 +444,9 @@ def all_at_once(swe, torch, dev, h, wind, particles, args, world_size, rank):
         e1.record(stream)
         w.sync()
         total += e0.elapsed_time(e1)
-    if world_size > 1:
-        t = torch.tensor([total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
+    total = max_over_ranks(total, dev)
     w.close()
-    return {"value": args.steps * world_size / (total / 1e3), "unit": UNIT, "ms_per_step": total / args.steps,
+    return {"value": whole_job_rate(args.steps, world_size, total), "unit": UNIT, "ms_per_step": total / args.steps,
             "lanes": particles, "kernel": "k_par_cycle (colour phases, cooperative)",
             "note": "all particles of a cycle in flight at once; mass conservation exact, but its height "
                     "histogram and spectrum drift from the sequential reference's (not the headline)"}
@@ -466,11 +479,8 @@ def e2e(w, swe, torch, stream, h, particles, args, world_size):
         e1.record(stream)
         w.sync()
         total += e0.elapsed_time(e1)
-    if world_size > 1:
-        t = torch.tensor([total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
-    return {"value": args.steps * world_size / (total / 1e3), "unit": UNIT,
+    total = max_over_ranks(total, "cuda")
+    return {"value": whole_job_rate(args.steps, world_size, total), "unit": UNIT,
             "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * 4 * n}
 
 

@@ -37,6 +37,7 @@
 // The grid barrier spins with an explicit deadline: a block that waits longer
 // than 2 s sets SWE_STATUS_TIMEOUT and an abort flag, and every block then
 // leaves the kernel at its next barrier, so the kernel always ends.
+#include <algorithm>
 #include <vector>
 
 #include "swe_device.cuh"
@@ -1180,9 +1181,12 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       const int qpos[5] = {12, 7, 17, 11, 13};  // positions in the 5x5 block
       unsigned need = 0, ready = 0, prev = 0;
       int32_t hv[5] = {0, 0, 0, 0, 0};
+      // (In a cluster a second barrier ends every step instead, so every
+      // word is final here and no tag is checked.)
+      const bool check = !kCluster && step > 0;
       if (ci >= 0) {
         need = 1u | (ix > 0 ? 2u : 0u) | (ix + 1 < nx ? 4u : 0u) | (iz > 0 ? 8u : 0u) | (iz + 1 < nz ? 16u : 0u);
-        if (step > 0) {
+        if (check) {
           unsigned rows = 0, cols = 0;
 #pragma unroll
           for (int d = -2; d <= 2; d++) {
@@ -1212,8 +1216,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         for (int q = 0; q < 5; q++) {
           if (((need & ~ready) >> q) & 1u) {
             const int qu = qpos[q] / 5 - 2, qw = qpos[q] % 5 - 2;
-            const unsigned want = step ? __popc(prev & near_mask(qu, qw)) + ((prev >> qpos[q]) & 1u) : 0u;
-            if (step == 0 || tag_ready(word_tag(wd[q]), pbase, want)) {
+            const unsigned want = check ? __popc(prev & near_mask(qu, qw)) + ((prev >> qpos[q]) & 1u) : 0u;
+            if (!check || tag_ready(word_tag(wd[q]), pbase, want)) {
               hv[q] = word_height(wd[q]);
               ready |= 1u << q;
             }
@@ -1442,12 +1446,21 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         if (!__any_sync(0xffffffffu, progressed)) __nanosleep(64);
       }
     }
+    if constexpr (kCluster) {
+      // the cheap hardware barrier makes every write of the step visible
+      // before the next flights (instead of checking tags in them)
+      cluster_barrier();
+      ph++;
+    }
     if (timer) {
       const unsigned long long now = global_ns();
       s_time[1] += now - s_time[2];
       s_time[2] = now;
     }
     if (done) break;
+    if constexpr (kCluster) {
+      if (aborted_before(A.gb, ph)) break;
+    }
   }
   // No CTA may leave while another can still read its shared memory.
   if constexpr (kCluster) cluster_barrier();
@@ -1711,9 +1724,18 @@ bool batch_fits(int lanes, int nx, int nz) {
 
 cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s) {
   if (count <= 0 || cycles <= 0) return cudaSuccess;
+  // Largest worlds first (cells x particles), so that the last clusters to
+  // finish are not the ones that started the longest worlds last.
+  std::vector<int> order((size_t)count);
+  for (int i = 0; i < count; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const double wa = (double)worlds[a].c.nx * worlds[a].c.nz * worlds[a].particles;
+    const double wb = (double)worlds[b].c.nx * worlds[b].c.nz * worlds[b].particles;
+    return wa > wb;
+  });
   std::vector<BatchItem> items((size_t)count);
   for (int i = 0; i < count; i++) {
-    const BatchWorld& w = worlds[i];
+    const BatchWorld& w = worlds[order[i]];
     CycleArgs& A = items[i].A;
     A.B = w.B;
     A.F = w.F;
