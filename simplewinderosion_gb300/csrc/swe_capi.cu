@@ -96,7 +96,7 @@ struct swe_world {
   int32_t* tape = nullptr;
   long long tape_len = 0;
   // parallel mode
-  int32_t* hq = nullptr;      // heights, then deltas, visit counts and stamps of even and odd steps (7 padded maps)
+  int32_t* hq = nullptr;      // heights; deltas, visit counts, owners of even and odd steps; 3 visited bitmaps
   long long* tq = nullptr;    // 4n
   unsigned long long* hw = nullptr;  // n height words of the cluster form
   void* pstate = nullptr;     // 2 buffers x 9 arrays x capacity
@@ -138,12 +138,14 @@ int use_device(swe_world* w) {
 
 // Parallel-mode buffers, grown to hold `particles` in flight.
 int ensure_parallel(swe_world* w, int particles) {
-  // heights, then exchange deltas, visit counts and cell stamps of even and
-  // odd steps, each padded to 64 elements so every map starts 256-byte aligned.
+  // heights, then exchange deltas and visit counts of even and odd steps,
+  // the cell owners of both, each padded to 64 elements so every map starts
+  // 256-byte aligned; then three visited bitmaps.
   const size_t stride = ((size_t)w->n + 63) & ~(size_t)63;
+  const size_t bw = ((size_t)(w->n + 128) / 32 + 2 + 63) & ~(size_t)63;
   if (!w->hq) {
-    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * 7 * stride));
-    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * 7 * stride, w->stream));
+    SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * (7 * stride + 3 * bw)));
+    SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * (7 * stride + 3 * bw), w->stream));
     SWE_CK(cudaMalloc(&w->tq, sizeof(long long) * 4 * w->n));
     SWE_CK(cudaMalloc(&w->hw, sizeof(unsigned long long) * w->n));
     SWE_CK(cudaMemsetAsync(w->tq, 0, sizeof(long long) * 4 * w->n, w->stream));
@@ -164,10 +166,12 @@ int ensure_parallel(swe_world* w, int particles) {
   B.hq = w->hq;
   B.dq = w->hq + stride;
   B.visits = w->hq + 2 * stride;
-  B.stamp = reinterpret_cast<uint32_t*>(w->hq + 3 * stride);
-  B.dq2 = w->hq + 4 * stride;
-  B.visits2 = w->hq + 5 * stride;
-  B.stamp2 = reinterpret_cast<uint32_t*>(w->hq + 6 * stride);
+  B.dq2 = w->hq + 3 * stride;
+  B.visits2 = w->hq + 4 * stride;
+  B.owner = w->hq + 5 * stride;
+  B.owner2 = w->hq + 6 * stride;
+  for (int k = 0; k < 3; k++) B.vbits[k] = reinterpret_cast<uint32_t*>(w->hq + 7 * stride + k * bw);
+  B.vbits_words = (long)((w->n + 128) / 32 + 2);
   B.hw = w->hw;
   for (int k = 0; k < 4; k++) B.tq[k] = w->tq + (size_t)k * w->n;
   int32_t* base = reinterpret_cast<int32_t*>(w->pstate);

@@ -41,8 +41,10 @@ struct ParallelBuffers {
   // last cascades finish
   int32_t* dq2;
   int32_t* visits2;
-  uint32_t* stamp;     // per cell, the step (from 1) in which it was last visited (even steps)
-  uint32_t* stamp2;    // the same for odd steps
+  int32_t* owner;      // the lowest lane id among a step's visitors of the cell (0x7FFFFFFF: none)
+  int32_t* owner2;
+  uint32_t* vbits[3];  // visited bitmaps of steps 0, 1, 2 mod 3 (cell i: bit 64 + i)
+  long vbits_words;    // words in each bitmap, (n + 128) / 32 + 2
   unsigned long long* hw;  // height words (fixed-point height, write tag)
   long long* tq[4];    // track accumulators (massflow, momx, momy, momz), 2^-32 units
   ParticleSoA state[2];

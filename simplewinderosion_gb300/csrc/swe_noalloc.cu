@@ -27,7 +27,9 @@ constexpr size_t kMaxCells = SWE_NOALLOC_MAX_CELLS;          // a multiple of 64
 constexpr size_t kMaxParticles = SWE_NOALLOC_MAX_PARTICLES;
 constexpr size_t kCountersBytes = align256(sizeof(swe::Counters));
 constexpr size_t kBarrierBytes = align256(sizeof(swe::GridBarrier));
-constexpr size_t kMapsBytes = 7 * kMaxCells * sizeof(int32_t);  // heights; deltas, owed cascades, stamps x2
+constexpr size_t kBitWords = ((kMaxCells + 128) / 32 + 2 + 63) & ~(size_t)63;  // one visited bitmap
+// heights; deltas, owed cascades, owners of even and odd steps; 3 bitmaps
+constexpr size_t kMapsBytes = (7 * kMaxCells + 3 * kBitWords) * sizeof(int32_t);
 constexpr size_t kTracksBytes = 4 * kMaxCells * sizeof(long long);   // track accumulators
 constexpr size_t kWordsBytes = kMaxCells * sizeof(unsigned long long);  // height words
 constexpr size_t kParticleBytes = 2 * 9 * kMaxParticles * sizeof(int32_t);  // two state buffers
@@ -122,10 +124,12 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   B.hq = maps;
   B.dq = maps + stride;
   B.visits = maps + 2 * stride;
-  B.stamp = reinterpret_cast<uint32_t*>(maps + 3 * stride);
-  B.dq2 = maps + 4 * stride;
-  B.visits2 = maps + 5 * stride;
-  B.stamp2 = reinterpret_cast<uint32_t*>(maps + 6 * stride);
+  B.dq2 = maps + 3 * stride;
+  B.visits2 = maps + 4 * stride;
+  B.owner = maps + 5 * stride;
+  B.owner2 = maps + 6 * stride;
+  for (int k = 0; k < 3; k++) B.vbits[k] = reinterpret_cast<uint32_t*>(maps + 7 * stride + k * kBitWords);
+  B.vbits_words = (long)((n + 128) / 32 + 2);
   B.hw = words;
   for (int k = 0; k < 4; k++) B.tq[k] = tracks + (size_t)k * n;
   for (int b = 0; b < 2; b++) {

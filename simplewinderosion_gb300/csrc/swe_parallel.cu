@@ -801,13 +801,18 @@ __device__ void ema_phase(const CycleArgs& A) {
   ema_cells<false>(A, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
 }
 
-// Before a bounded-lanes cycle: height words with tag 0, visited stamps and
-// track accumulators cleared, for cells i0, i0 + stride, ...
+// Before a bounded-lanes cycle: height words with tag 0, owners none,
+// visited bitmaps and track accumulators cleared, for cells i0, i0 + stride, ...
 __device__ void prologue_cells(const ParallelBuffers& B, long n, long i0, long stride) {
+  for (long i = i0; i < B.vbits_words; i += stride) {
+    B.vbits[0][i] = 0;
+    B.vbits[1][i] = 0;
+    B.vbits[2][i] = 0;
+  }
   for (long i = i0; i < n; i += stride) {
     B.hw[i] = (unsigned long long)(uint32_t)B.hq[i];
-    B.stamp[i] = 0;
-    B.stamp2[i] = 0;
+    B.owner[i] = 0x7FFFFFFF;
+    B.owner2[i] = 0x7FFFFFFF;
     B.tq[0][i] = 0; B.tq[1][i] = 0; B.tq[2][i] = 0; B.tq[3][i] = 0;
   }
 }
@@ -1010,6 +1015,38 @@ __host__ __device__ constexpr unsigned near_mask(int qu, int qw) {
 // kCluster: the 16 CTAs of one cluster (cluster barriers, lane counts over
 // distributed shared memory); otherwise one CTA per SM of a cooperative grid
 // (grid barriers, lane counts in global memory).
+// Visited bitmaps: cell i is bit 64 + i (64 bits of padding at both ends, so
+// that the 5-bit runs read below never leave the array).
+__device__ __forceinline__ void mark_visited(uint32_t* bm, long ci) {
+  atomicOr(bm + ((ci + 64) >> 5), 1u << ((ci + 64) & 31));
+}
+
+// The visited bits of the 5x5 block around cell (x, z) (bit (du+2)*5 + dw+2),
+// unmasked: rows off the map read the cell's own row, columns off the map
+// read bits of the neighbouring rows; the caller masks both. The ten loads
+// (load) and the assembly (bits) are split so that callers can issue other
+// loads in between.
+struct BlockBits {
+  uint32_t lo[5], hi[5];
+  unsigned sh[5];
+  __device__ __forceinline__ void load(const uint32_t* bm, int x, int z, int nx, int nz) {
+#pragma unroll
+    for (int d = 0; d < 5; d++) {
+      const int xr = (x + d - 2 >= 0 && x + d - 2 < nx) ? x + d - 2 : x;
+      const long b = (long)xr * nz + z - 2 + 64;
+      sh[d] = (unsigned)(b & 31);
+      lo[d] = __ldcg(bm + (b >> 5));
+      hi[d] = __ldcg(bm + (b >> 5) + 1);
+    }
+  }
+  __device__ __forceinline__ unsigned bits() const {
+    unsigned m = 0;
+#pragma unroll
+    for (int d = 0; d < 5; d++) m |= (__funnelshift_r(lo[d], hi[d], sh[d]) & 31u) << (5 * d);
+    return m;
+  }
+};
+
 template <bool kCluster>
 __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32_t* dyn) {
   __shared__ int s_free[2];            // free lanes of this CTA by step parity, read by the other CTAs
@@ -1059,6 +1096,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   for (int s = 0; s < kClusterMaxSlots; s++)
     if (s < slots && s * T + t < Lr) lanes_mask |= 1u << s;
   unsigned live = 0;
+  const int lane_id0 = (int)r * cap;  // lane slot j of this CTA has id lane_id0 + j
 
   const bool timer = r == 0 && t == 0;
   if (timer) {
@@ -1141,7 +1179,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   // the owned cells absorb their deltas and run their cascades. A thread goes
   // on to its next flight as soon as its own cascades are done: the deltas,
   // visit counts and stamps of consecutive steps live in separate maps.
-  for (unsigned step = 0;; step++) {
+  unsigned rot = 0;  // step mod 3
+  for (unsigned step = 0;; step++, rot = rot == 2 ? 0 : rot + 1) {
     if (cst.transfers > 0x40000000u || cst.cascades > 0x40000000u || steps > 0x40000000u) {
       atomicAdd(&cnt->transfers, (unsigned long long)cst.transfers);
       atomicAdd(&cnt->cascades, (unsigned long long)cst.cascades);
@@ -1153,13 +1192,21 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
     const unsigned odd = step & 1u;
     const unsigned vmark = step + 1;     // visited stamp of this step
     const unsigned tbase = 16u * vmark;  // tag base of this step
-    uint32_t* stamp = odd ? B.stamp2 : B.stamp;
-    const uint32_t* stamp_prev = odd ? B.stamp : B.stamp2;
+    // visited bitmaps by step mod 3: this step's, the previous step's, and
+    // the one two steps back, cleared now (its last readers were the
+    // previous step's flights; its next writers fly after this step's barrier)
+    uint32_t* vb = B.vbits[rot];
+    const uint32_t* vb_prev = B.vbits[rot == 0 ? 2 : rot - 1];
+    {
+      uint32_t* vb_clear = B.vbits[rot == 2 ? 0 : rot + 1];
+      for (long i = (long)r * T + t; i < B.vbits_words; i += (long)nb * T) vb_clear[i] = 0;
+    }
     int32_t* visits = odd ? B.visits2 : B.visits;
     int32_t* dq = odd ? B.dq2 : B.dq;
+    int32_t* owner = odd ? B.owner2 : B.owner;
 
     // Fly.
-    unsigned owned = 0;  // bit s: slot s owns its cell this step
+    unsigned flew = 0;  // bit s: slot s flew this step (its cell is in s_own)
 #pragma unroll
     for (int s = 0; s < kClusterMaxSlots; s++) {
       if (s >= slots) break;
@@ -1179,8 +1226,9 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       // next to it (from the previous step's stamps of the 5x5 block).
       const long nbr[5] = {0, -(long)nz, (long)nz, -1, 1};
       const int qpos[5] = {12, 7, 17, 11, 13};  // positions in the 5x5 block
-      unsigned need = 0, ready = 0, prev = 0;
+      unsigned need = 0, ready = 0, prev = 0, inm = 0;
       int32_t hv[5] = {0, 0, 0, 0, 0};
+      BlockBits pb;
       // (In a cluster a second barrier ends every step instead, so every
       // word is final here and no tag is checked.)
       const bool check = !kCluster && step > 0;
@@ -1193,25 +1241,19 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
             rows |= (ix + d >= 0 && ix + d < nx) ? 1u << (d + 2) : 0u;
             cols |= (iz + d >= 0 && iz + d < nz) ? 1u << (d + 2) : 0u;
           }
-          unsigned inm = 0;
 #pragma unroll
           for (int d = 0; d < 5; d++) inm |= ((rows >> d) & 1u) ? cols << (5 * d) : 0u;
-          unsigned sv[25];
-#pragma unroll
-          for (int k = 0; k < 25; k++)
-            sv[k] = __ldcg(stamp_prev + (((inm >> k) & 1u) ? ci + (k / 5 - 2) * nz + (k % 5 - 2) : ci));
-#pragma unroll
-          for (int k = 0; k < 25; k++) prev |= sv[k] == step ? 1u << k : 0u;
-          prev &= inm;
+          pb.load(vb_prev, ix, iz, nx, nz);
         }
       }
       const unsigned pbase = 16u * step;  // tag base of the previous step
       unsigned long long t_wait = 0;
-      for (;;) {
+      for (bool first = true;; first = false) {
         unsigned long long wd[5];
 #pragma unroll
         for (int q = 0; q < 5; q++)
           wd[q] = (((need & ~ready) >> q) & 1u) ? ld_relaxed64(HW + ci + nbr[q]) : 0ull;
+        if (first && check && ci >= 0) prev = pb.bits() & inm;
 #pragma unroll
         for (int q = 0; q < 5; q++) {
           if (((need & ~ready) >> q) & 1u) {
@@ -1244,12 +1286,14 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           ci = -1;
         if (ci >= 0) {
           steps++;
-          if (atomicAdd(visits + ci, 1) == 0) {
-            __stcg(stamp + ci, vmark);
-            s_own[j] = (int)ci;
-            s_ox[j] = ix;
-            owned |= 1u << s;
-          }
+          // One cascade owed to the cell; the lowest lane id among the
+          // cell's visitors becomes its owner (both without a round trip).
+          atomicAdd(visits + ci, 1);
+          atomicMin(owner + ci, lane_id0 + j);
+          mark_visited(vb, ci);
+          s_own[j] = (int)ci;
+          s_ox[j] = ix;
+          flew |= 1u << s;
           PI(1, j) = p.age; PI(2, j) = p.sed_q;
           PF(3, j) = p.px; PF(4, j) = p.py; PF(5, j) = p.pz;
           PF(6, j) = p.vx; PF(7, j) = p.vy; PF(8, j) = p.vz;
@@ -1302,18 +1346,28 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       nid += refill;
     }
 
-    // The owned cells' deltas: the first write of each in the step.
+    // Owners and their cells' deltas: the first write of each cell in the
+    // step, before any cascade waits. Every lane that flew loads its cell's
+    // owner, visit, delta and word entries in one batch; the owner clears the
+    // owner, visit and delta entries (a visitor reading the owner entry after
+    // that sees no match either).
+    unsigned owned = 0;
 #pragma unroll
     for (int s = 0; s < kClusterMaxSlots; s++) {
-      if ((owned >> s) & 1u) {
+      if ((flew >> s) & 1u) {
         const int ci = s_own[s * T + t];
+        const int ow = __ldcg(owner + ci);
         const int v = __ldcg(visits + ci);
         const int32_t d = __ldcg(dq + ci);
         const unsigned long long w = ld_relaxed64(HW + ci);
-        s_vis[s * T + t] = v;
-        __stcg(visits + ci, 0);
-        __stcg(dq + ci, 0);
-        st_relaxed64(HW + ci, make_word(wrap_add(word_height(w), d), tbase + 1));
+        if (ow == lane_id0 + s * T + t) {
+          owned |= 1u << s;
+          s_vis[s * T + t] = v;
+          __stcg(visits + ci, 0);
+          __stcg(dq + ci, 0);
+          __stcg(owner + ci, 0x7FFFFFFF);
+          st_relaxed64(HW + ci, make_word(wrap_add(word_height(w), d), tbase + 1));
+        }
       }
     }
     // Cascades of the owned cells. Each lane takes its cells in colour order
@@ -1330,8 +1384,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       unsigned long long t_wait = 0;
       for (;;) {
         bool progressed = false;
-        bool fresh = false;  // a new cell in hand: its stamps were loaded in this pass
-        unsigned sv[25];
+        bool fresh = false;  // a new cell in hand: its visited bits were loaded in this pass
+        BlockBits cb;
         if (cs < 0 && todo && !gave_up) {
           // the lowest-colour cell left
           if (slots == 1) {
@@ -1363,13 +1417,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           inmask = 0;
 #pragma unroll
           for (int d = 0; d < 5; d++) inmask |= ((rows >> d) & 1u) ? cols << (5 * d) : 0u;
-          // Stamps of the 5x5 block around (cells off the map read the
-          // cell's own stamp and are masked below).
-#pragma unroll
-          for (int k = 0; k < 25; k++) {
-            const int du = k / 5 - 2, dw = k % 5 - 2;
-            sv[k] = __ldcg(stamp + (((inmask >> k) & 1u) ? ci + du * nz + dw : ci));
-          }
+          // visited bits of the 5x5 block around (assembled below)
+          cb.load(vb, x, z, nx, nz);
           // the 3x3 neighbourhood's in-map cells (bit 3u+w)
           okmask = 0;
 #pragma unroll
@@ -1391,12 +1440,10 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         }
         if (fresh) {
           // visited cells of the 5x5 block, and those of lower colour
-          visited = 0;
-#pragma unroll
-          for (int k = 0; k < 25; k++) visited |= sv[k] == vmark ? 1u << k : 0u;
-          visited = (visited & inmask) | (1u << 12);
+          visited = (cb.bits() & inmask) | (1u << 12);
           lower = visited & s_lower[(x % 3) * 3 + z % 3];
         }
+
         if (cs >= 0) {
           // Take the words whose tags show every earlier write (the cell's
           // own delta if visited, the cascades of the lower-colour visited
