@@ -38,7 +38,7 @@ extern "C" {
 #define SWE_STATUS_NONFINITE 0x1u  /* a particle produced NaN/Inf and was retired */
 #define SWE_STATUS_RANGE 0x2u      /* a fixed-point height left its safe range     */
 #define SWE_STATUS_TAPE 0x4u       /* an ordered-mode rand tape ran out            */
-#define SWE_STATUS_TIMEOUT 0x8u    /* a grid barrier gave up waiting; cycle aborted */
+#define SWE_STATUS_TIMEOUT 0x8u    /* a wait (barrier or cell tag) gave up; cycle aborted */
 
 /* Simulation constants; swe_params_default() gives the reference's values.
  * Replaces the statics Wind::maxAge/boundarylayer/suspension/gravity
@@ -240,9 +240,12 @@ int swe_world_set_stream(swe_world* w, void* stream);
  * counterpart (the reference has no timing). */
 int swe_world_kernel_times(swe_world* w, double* fly_ms, double* cascade_ms);
 
-/* The same clock per phase of the parallel cycle kernel, ms summed over the
+/* The same clock per phase of the parallel cycle kernels, ms summed over the
  * last swe_world_erode call, in the order: spawn, fly, (unused), colour 0..8,
- * ema (n <= 13 values written). */
+ * ema (n <= 13 values written). The all-at-once kernel fills every slot; the
+ * bounded-lanes kernel (the default) has no colour phases and reports its
+ * flights and barrier under fly and its absorbs and cascades under colour 0
+ * (its spawns, map sweeps and EMA are not timed). */
 int swe_world_phase_times(swe_world* w, double* ms, int n);
 
 /* Cascade work of the last parallel swe_world_erode call: World::cascade
@@ -267,7 +270,7 @@ int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host
  * parallel erode cycles of `particles_per_cycle` particles (same results as a
  * world whose random-number cycle counter is `first_cycle`), enqueued on
  * `stream` (NULL: the default stream). The scratch it needs lives in one
- * static device array, about 21.5 MB on every GPU that loads the library,
+ * static device array, about 21.6 MB on every GPU that loads the library,
  * held until the process exits; its limits are SWE_NOALLOC_MAX_CELLS cells
  * and SWE_NOALLOC_MAX_PARTICLES particles per cycle, and larger requests fail
  * with SWE_ERR_INVALID. The first call on a device looks up that array's
