@@ -36,8 +36,8 @@ struct ParallelBuffers {
   int32_t* hq;         // fixed-point heights
   int32_t* dq;         // exchange deltas pending for the cascade passes (zero between steps)
   int32_t* visits;     // cascades owed per cell (zero between steps)
-  // bounded-lanes form: the maps of odd steps (the even steps use dq, visits
-  // and stamp), so that a step's flights can start while the previous step's
+  // bounded-lanes form: the maps of odd steps (the even steps use dq and
+  // visits), so that a step's flights can start while the previous step's
   // last cascades finish
   int32_t* dq2;
   int32_t* visits2;

@@ -909,42 +909,54 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
 }
 
 // ---------------------------------------------------------------------------
-// Single-cluster form of the cycle, for a bounded number of particles in
-// flight.
+// Bounded-lanes form of the cycle (k_par_lanes), for a bounded number of
+// particles in flight.
 //
-// With few particles in flight a step is short, and the grid kernel's eleven
-// grid-wide barriers per step dominate it. Here one thread-block cluster of
-// 16 CTAs runs the steps of the cycle: each thread holds up to
-// kClusterMaxSlots lanes (particle state in shared memory), and a step has
-// two cluster barriers (hardware, a fraction of a microsecond):
-//   B1   every CTA's count of free lanes is read over distributed shared
-//        memory and the cycle's next particles take the free lanes (the same
-//        ids as in the grid kernel: the set of particles flying in a step is
-//        identical, only their lanes differ);
-//   fly  every particle flies against the step-start heights; the first
-//        particle to reach a cell in the step (its visit counter was 0) makes
-//        its thread the cell's owner and stamps the cell visited;
-//   B2   then each owner adds the cell's pending delta (H += D) and runs the
-//        cell's owed cascades.
+// With few particles in flight a step is short, and the colour-phase
+// kernel's eleven grid-wide barriers per step dominate it. Here each thread
+// holds up to kClusterMaxSlots lanes (particle state in shared memory) and a
+// step has one barrier: one 16-CTA thread-block cluster (hardware barrier,
+// lane counts over distributed shared memory) for up to 4,096 lanes, else
+// one CTA per SM of a cooperative grid (a flat barrier whose arrival atomic
+// also sums the free lanes). A step:
+//   fly      every particle flies against the heights the previous step left;
+//            it adds one to its cell's visit count, marks the cell in the
+//            step's visited bitmap and offers its lane id to the cell's owner
+//            entry (atomicMin: the lowest id owns the cell), all without a
+//            round trip;
+//   barrier  every CTA learns the free lanes, and the cycle's next particles
+//            take them (the same ids as in the colour-phase kernel: the set
+//            of particles flying in a step is identical, only their lanes
+//            differ);
+//   cascade  each owner adds the cell's pending delta (H += D) and runs the
+//            cell's owed cascades.
 // The cascades are ordered cell by cell, reproducing the colour phases
 // exactly: two cascades interact only if their 3x3 neighbourhoods overlap
 // (cells at most 2 apart), and then the one of lower colour (x%3, z%3) runs
 // first; every delta is added before any cascade reads the cell. Heights live
 // here as 64-bit words, the fixed-point height in the low half and a tag in
 // the high half: 16*(step+1) + the number of writes the cell has had in the
-// step (its delta, then cascades). From the visited stamps of the 5x5 cells
+// step (its delta, then cascades). From the visited bits of the 5x5 cells
 // around it, a cascade knows how many writes each cell of its 3x3 must have
 // had before it reads it (the cell's own delta if it was visited, and the
 // cascades of lower-colour visited cells next to it); it reads the words
 // until their tags say so, then writes each cell back with its tag plus one.
+// In the grid form the next step's flights check the tags of their five
+// cells the same way (every write of the previous step), so no barrier
+// separates a step's cascades from the next flights; the deltas, visit
+// counts and owners of even and odd steps live in separate maps and the
+// visited bitmaps rotate by step mod 3. In the cluster form a second
+// hardware barrier ends every step instead.
 // A value and its tag are written together by one 64-bit store, so the
 // ordering rests on the coherence of single words alone: no memory fences
 // (which serialise on an SM) are needed. Every wait is on a delta or on a
 // lower colour, so the waits cannot form a cycle; a thread handles its cells
-// in colour order, and the CTAs of a cluster are co-resident, so every wait
-// ends. Each wait still has a 2 s deadline: past it the thread sets
-// SWE_STATUS_TIMEOUT and the abort flag, tagged with the barrier count, and
-// every thread leaves the step loop after the same barrier.
+// in colour order, the polling loops are warp-uniform (a lane that is not
+// ready polls again on the next pass, so it never holds up a lane of its own
+// warp), and the CTAs are co-resident, so every wait ends. Each wait still
+// has a 2 s deadline: past it the thread sets SWE_STATUS_TIMEOUT and the
+// abort flag, tagged with the barrier count, and every thread leaves the step
+// loop after the same barrier.
 // ---------------------------------------------------------------------------
 constexpr int kClusterCtas = 16;
 constexpr int kClusterMaxThreads = 256;  // up to 255 registers a thread
@@ -1178,7 +1190,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   // which the free lanes are counted; the next particles take the free lanes;
   // the owned cells absorb their deltas and run their cascades. A thread goes
   // on to its next flight as soon as its own cascades are done: the deltas,
-  // visit counts and stamps of consecutive steps live in separate maps.
+  // visit counts and owners of consecutive steps live in separate maps.
   unsigned rot = 0;  // step mod 3
   for (unsigned step = 0;; step++, rot = rot == 2 ? 0 : rot + 1) {
     if (cst.transfers > 0x40000000u || cst.cascades > 0x40000000u || steps > 0x40000000u) {
@@ -1190,8 +1202,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       steps = 0;
     }
     const unsigned odd = step & 1u;
-    const unsigned vmark = step + 1;     // visited stamp of this step
-    const unsigned tbase = 16u * vmark;  // tag base of this step
+    const unsigned tbase = 16u * (step + 1);  // tag base of this step
     // visited bitmaps by step mod 3: this step's, the previous step's, and
     // the one two steps back, cleared now (its last readers were the
     // previous step's flights; its next writers fly after this step's barrier)
@@ -1223,7 +1234,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       // The five cells' words (bits 0..4: the cell, x-1, x+1, z-1, z+1),
       // each read until its tag shows every write of the previous step: the
       // cell's delta if it was visited, and the cascades of the visited cells
-      // next to it (from the previous step's stamps of the 5x5 block).
+      // next to it (from the previous step's visited bits of the 5x5 block).
       const long nbr[5] = {0, -(long)nz, (long)nz, -1, 1};
       const int qpos[5] = {12, 7, 17, 11, 13};  // positions in the 5x5 block
       unsigned need = 0, ready = 0, prev = 0, inm = 0;
@@ -1429,7 +1440,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           t_wait = 0;
           fresh = true;
         }
-        // The words not taken yet, loaded in the same batch as the stamps
+        // The words not taken yet, loaded in the same batch as the visited bits
         // (taken or off-map words read the cell's own word and are masked).
         unsigned long long wd[9];
 #pragma unroll
