@@ -19,6 +19,7 @@ ENSEMBLE = [
     (96, 96, 9000, (1.0, 0.0, 0.0), 24, 2048, 5),
     (33, 70, 1200, swe.wind_direction(-1.0, 0.0, 2.0), 20, 0, 6),
     (128, 128, 16384, WIND_101, 16, 0, 7),
+    (128, 128, 16384, (0.0, 0.0, -1.0), 16, -1, 9),  # 16,384 in flight: four lanes a thread in the cluster
     (160, 96, 20000, (0.0, 0.0, 1.0), 24, -1, 8),  # 20,000 in flight: its own launch
 ]
 
