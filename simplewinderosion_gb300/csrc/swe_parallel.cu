@@ -143,67 +143,44 @@ __device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
   return s_ok != 0;
 }
 
-__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ unsigned long long atom_add_acq_rel64(unsigned long long* p, unsigned long long v) {
-  unsigned long long old;
-  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
-  return old;
-}
-
-__device__ __forceinline__ void st_release64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-__device__ __forceinline__ void st_relaxed64u(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-// The flat barrier whose arrivals also add up one count per block: *below
-// gets the sum over the blocks that arrived before this one, *total the sum
-// over all blocks (the arrival order stands in for a block order).
-__device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned mine, unsigned* below,
-                              unsigned* total) {
+// A grid barrier of one atomic per block whose arrivals also add up one
+// count per block. Block 0 adds 2^31 - (blocks - 1) to the flip counter and
+// every other block 1, so the counter's top bit flips exactly when the last
+// block arrives and each block waits for the flip relative to the value its
+// own arrival returned: no generation word to read first or to publish last.
+// The counts go to sums[phase] (phase = step mod 3): *below gets the sum over
+// the blocks whose counts landed before this one's (an arrival order standing
+// in for a block order), *total the sum over all blocks, read after the flip.
+// Block 0 clears sums[phase + 1 mod 3] before it arrives: that counter's last
+// total was read two barriers ago, and its next counts come after this one.
+__device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned phase, unsigned mine,
+                              unsigned* below, unsigned* total) {
   __shared__ int s_ok;
   __shared__ unsigned s_below, s_total;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned g = (unsigned)(ld_acquire64(&gb->gen64) >> 32);
-    const unsigned long long old = atom_add_acq_rel64(&gb->count64, (1ull << 32) | mine);
-    const unsigned b = (unsigned)old;
-    unsigned tot = 0;
-    if ((unsigned)(old >> 32) == gridDim.x - 1) {
-      tot = b + mine;
-      st_relaxed64u(&gb->count64, 0ull);
-      st_release64(&gb->gen64, ((unsigned long long)(g + 1u) << 32) | tot);
-    } else {
-      const unsigned long long t0 = global_ns();
-      for (;;) {
-        const unsigned long long w = ld_acquire64(&gb->gen64);
-        if ((unsigned)(w >> 32) != g) {
-          tot = (unsigned)w;
-          break;
-        }
-        if (ld_acquire(&gb->abort)) {
-          ok = 0;
-          break;
-        }
-        if (global_ns() - t0 > kBarrierLimitNs) {
-          atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
-          atomicExch(&gb->abort, 1u);
-          ok = 0;
-          break;
-        }
+    unsigned* sum = &gb->sums[32 * phase];
+    if (blockIdx.x == 0) st_relaxed(&gb->sums[32 * (phase == 2 ? 0 : phase + 1)], 0u);
+    const unsigned b = atomicAdd(sum, mine);
+    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
+    const unsigned old = atom_add_acq_rel(&gb->flip, add);
+    const unsigned long long t0 = global_ns();
+    while (((ld_acquire(&gb->flip) ^ old) & 0x80000000u) == 0) {
+      if (ld_acquire(&gb->abort)) {
+        ok = 0;
+        break;
+      }
+      if (global_ns() - t0 > kBarrierLimitNs) {
+        atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
+        atomicExch(&gb->abort, 1u);
+        ok = 0;
+        break;
       }
     }
     if (ld_acquire(&gb->abort)) ok = 0;
     s_below = b;
-    s_total = tot;
+    s_total = ld_acquire(sum);
     s_ok = ok;
   }
   __syncthreads();
@@ -1336,7 +1313,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       }
     } else {
       unsigned below = 0, tot = 0;
-      if (!grid_sync_sum(A.gb, &cnt->status, (unsigned)btotal, &below, &tot)) break;
+      if (!grid_sync_sum(A.gb, &cnt->status, rot, (unsigned)btotal, &below, &tot)) break;
       ph++;
       total_free = (int)tot;
       base = (int)below;

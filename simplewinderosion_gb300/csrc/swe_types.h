@@ -62,12 +62,13 @@ struct GridBarrier {
   unsigned int pad[29];
   unsigned int leaf[16 * 32];  // block arrivals per leaf, one 128-byte line each
   int lanes_free[1024];        // bounded-lanes kernel: free lanes per block, this step
-  // A second flat barrier whose arrivals also sum a per-block count:
-  // arrivals << 32 | running sum, and generation << 32 | the step's total.
-  unsigned long long count64;
-  unsigned long long pad64a[15];
-  unsigned long long gen64;
-  unsigned long long pad64b[15];
+  // A second barrier, one arrival atomic per block: every block adds 1 but
+  // block 0, which adds 2^31 - (blocks - 1), so the top bit flips when the
+  // last block arrives; and three counters (one per step mod 3) summing a
+  // per-block count on the way.
+  unsigned int flip;
+  unsigned int pad3[31];
+  unsigned int sums[3 * 32];  // one 128-byte line each
 };
 
 // Particle state of the parallel mode, structure of arrays.
