@@ -1214,7 +1214,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       // next to it (from the previous step's visited bits of the 5x5 block).
       const long nbr[5] = {0, -(long)nz, (long)nz, -1, 1};
       const int qpos[5] = {12, 7, 17, 11, 13};  // positions in the 5x5 block
-      unsigned need = 0, ready = 0, prev = 0, inm = 0;
+      unsigned need = 0, ready = 0, prev = 0, inm = 0, fwant = 0;
       int32_t hv[5] = {0, 0, 0, 0, 0};
       BlockBits pb;
       // (In a cluster a second barrier ends every step instead, so every
@@ -1241,12 +1241,18 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
 #pragma unroll
         for (int q = 0; q < 5; q++)
           wd[q] = (((need & ~ready) >> q) & 1u) ? ld_relaxed64(HW + ci + nbr[q]) : 0ull;
-        if (first && check && ci >= 0) prev = pb.bits() & inm;
+        if (first && check && ci >= 0) {
+          prev = pb.bits() & inm;
+#pragma unroll
+          for (int q = 0; q < 5; q++) {
+            const int qu = qpos[q] / 5 - 2, qw = qpos[q] % 5 - 2;
+            fwant |= (__popc(prev & near_mask(qu, qw)) + ((prev >> qpos[q]) & 1u)) << (4 * q);
+          }
+        }
 #pragma unroll
         for (int q = 0; q < 5; q++) {
           if (((need & ~ready) >> q) & 1u) {
-            const int qu = qpos[q] / 5 - 2, qw = qpos[q] % 5 - 2;
-            const unsigned want = check ? __popc(prev & near_mask(qu, qw)) + ((prev >> qpos[q]) & 1u) : 0u;
+            const unsigned want = (fwant >> (4 * q)) & 15u;
             if (!check || tag_ready(word_tag(wd[q]), pbase, want)) {
               hv[q] = word_height(wd[q]);
               ready |= 1u << q;
@@ -1369,6 +1375,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       int cs = -1;            // slot of the cell in hand
       int ci = 0, x = 0, z = 0;
       unsigned visited = 0, lower = 0, ready = 0, okmask = 0, inmask = 0;
+      unsigned long long wants = 0;  // 4 bits per word of the 3x3: the writes it must have had
       unsigned long long t_wait = 0;
       for (;;) {
         bool progressed = false;
@@ -1430,6 +1437,13 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           // visited cells of the 5x5 block, and those of lower colour
           visited = (cb.bits() & inmask) | (1u << 12);
           lower = visited & s_lower[(x % 3) * 3 + z % 3];
+          wants = 0;
+#pragma unroll
+          for (int q = 0; q < 9; q++) {
+            const int u = q / 3, w = q % 3;
+            const unsigned want = __popc(lower & near_mask(u - 1, w - 1)) + ((visited >> ((u + 1) * 5 + w + 1)) & 1u);
+            wants |= (unsigned long long)want << (4 * q);
+          }
         }
 
         if (cs >= 0) {
@@ -1438,9 +1452,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           // cells next to it).
 #pragma unroll
           for (int q = 0; q < 9; q++) {
-            const int u = q / 3, w = q % 3;
             const bool need = ((okmask & ~ready) >> q) & 1u;
-            const unsigned want = __popc(lower & near_mask(u - 1, w - 1)) + ((visited >> ((u + 1) * 5 + w + 1)) & 1u);
+            const unsigned want = (unsigned)(wants >> (4 * q)) & 15u;
             if (need && tag_ready(word_tag(wd[q]), tbase, want)) {
               N[q] = word_height(wd[q]);
               ready |= 1u << q;
@@ -1453,8 +1466,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
             for (int q = 0; q < 9; q++) {
               const int u = q / 3, w = q % 3;
               if ((okmask >> q) & 1u) {
-                const unsigned want =
-                    __popc(lower & near_mask(u - 1, w - 1)) + ((visited >> ((u + 1) * 5 + w + 1)) & 1u);
+                const unsigned want = (unsigned)(wants >> (4 * q)) & 15u;
                 st_relaxed64(HW + ci + (u - 1) * nz + (w - 1), make_word(N[q], tbase + want + 1));
               }
             }
