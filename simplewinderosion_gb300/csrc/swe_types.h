@@ -61,7 +61,6 @@ struct GridBarrier {
   unsigned int abort;  // set by a block that gave up waiting
   unsigned int pad[29];
   unsigned int leaf[16 * 32];  // block arrivals per leaf, one 128-byte line each
-  int lanes_free[1024];        // bounded-lanes kernel: free lanes per block, this step
   // A second barrier, one arrival atomic per block: every block adds 1 but
   // block 0, which adds 2^31 - (blocks - 1), so the top bit flips when the
   // last block arrives; and three counters (one per step mod 3) summing a
