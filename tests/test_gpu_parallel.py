@@ -39,6 +39,12 @@ def _pair(nx, nz, seed, wind=WIND_101, frac_bits=24, wseed=5, lanes=0):
     (160, 96, 45000, 1, (0.0, 0.0, -1.0), 24, 40000),
     # more lanes than that form holds: the colour-phase kernel
     (64, 64, 200000, 1, WIND_101, 24, -1),
+    # degenerate shapes: one row, one column, a thin strip on one CTA per SM,
+    # and a single lane (one particle at a time)
+    (1, 50, 200, 2, WIND_101, 24, 0),
+    (50, 1, 200, 2, (1.0, 0.0, 0.0), 24, 0),
+    (3, 2000, 6000, 1, (0.0, 0.0, 1.0), 16, 5000),
+    (40, 40, 300, 1, WIND_101, 16, 1),
 ])
 def test_parallel_bitwise_vs_cpu_model(nx, nz, particles, cycles, wind, frac_bits, lanes):
     port, w = _pair(nx, nz, 7, wind, frac_bits, lanes=lanes)
