@@ -151,7 +151,11 @@ int swe_world_device_field(swe_world* w, swe_field f, void** dev_ptr);
 
 /* World::erode(particles_per_cycle), `cycles` times (world.hpp:36-77):
  * track reset, particle flights, EMA update of massflow/momentum. Asynchronous
- * on the world's stream. */
+ * on the world's stream. A PARALLEL call can be captured into a CUDA graph on
+ * the world's stream once a first PARALLEL call with the same particle count
+ * has run outside the capture (it allocates the buffers); every replay of
+ * the graph is one more erode cycle (the cycle counter that keys the random
+ * numbers lives on the device). */
 int swe_world_erode(swe_world* w, int cycles, int particles_per_cycle, swe_mode mode);
 
 /* An ensemble: `cycles` PARALLEL erode cycles of worlds[i] with
@@ -163,7 +167,7 @@ int swe_world_erode(swe_world* w, int cycles, int particles_per_cycle, swe_mode 
  * each cluster taking the next world from a queue; the others run on their
  * own streams. All worlds must live on one device and be distinct. Returns
  * after the persistent launch has completed (the other worlds' cycles stay
- * asynchronous on their streams). Extends the reference, which erodes one
+ * asynchronous on their streams); not for stream capture. Extends the reference, which erodes one
  * world (world.hpp:36-77). */
 int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle);
 
