@@ -52,7 +52,6 @@ constexpr float kSqrt2 = 1.41421354f;  // sqrtf(2.0f), correctly rounded
 constexpr int kCycleThreads = 256;
 constexpr int kCycleBlocksPerSm = 4;  // 64 registers per thread, no spills
 constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
-constexpr unsigned kBarrierLeaves = 16;
 
 __device__ __forceinline__ float fx2f(int32_t q, float inv) { return __int2float_rn(q) * inv; }
 __device__ __forceinline__ int32_t wrap_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
@@ -79,12 +78,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-__device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned v) {
-  unsigned old;
-  asm volatile("atom.release.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
-
 __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
   unsigned old;
   asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
@@ -95,45 +88,34 @@ __device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
   asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Grid-wide barrier of a cooperative launch (all blocks co-resident), as a
-// two-level tree of release/acquire atomics (no separate fences): thread 0
-// of each block arrives on one of kBarrierLeaves leaf counters (separate
-// 128-byte lines, so arrivals do not serialise on one address); the last
-// arrival at a leaf arrives at the root; the last arrival at the root resets
-// it and bumps the generation everyone waits on with acquire loads. The
-// block barriers before and after carry the rest of the block's threads.
-// Returns false if the kernel must stop.
+// Grid-wide barrier of a cooperative launch (all blocks co-resident), one
+// arrival atomic per block: every block adds 1 to the flip counter but block
+// 0, which adds 2^31 - (blocks - 1), so the counter's top bit flips exactly
+// when the last block arrives; each block waits for the flip relative to the
+// value its own arrival returned (release/acquire atomics, no separate
+// fences, no generation word to read first or to publish last). Thread 0
+// arrives for its block; the block barriers before and after carry the rest
+// of the block's threads. Every wait has a 2 s deadline, after which the
+// block sets SWE_STATUS_TIMEOUT and the abort flag; returns false if the
+// kernel must stop.
 __device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned g = ld_acquire(&gb->gen);
-    const unsigned leaf = blockIdx.x % kBarrierLeaves;
-    const unsigned leaf_size = gridDim.x / kBarrierLeaves + (leaf < gridDim.x % kBarrierLeaves ? 1u : 0u);
-    const unsigned nleaves = gridDim.x < kBarrierLeaves ? gridDim.x : kBarrierLeaves;
-    bool last = false;
-    if (atom_add_acq_rel(&gb->leaf[leaf * 32], 1u) == leaf_size - 1) {
-      st_relaxed(&gb->leaf[leaf * 32], 0u);
-      last = atom_add_acq_rel(&gb->count, 1u) == nleaves - 1;
-    }
-    if (last) {
-      st_relaxed(&gb->count, 0u);
-      atom_add_release(&gb->gen, 1u);
-    } else {
-      const unsigned long long t0 = global_ns();
-      while (ld_acquire(&gb->gen) == g) {
-        if (ld_acquire(&gb->abort)) {
-          ok = 0;
-          break;
-        }
-        if (global_ns() - t0 > kBarrierLimitNs) {
-          atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
-          atomicExch(&gb->abort, 1u);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
+    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
+    const unsigned old = atom_add_acq_rel(&gb->flip, add);
+    const unsigned long long t0 = global_ns();
+    while (((ld_acquire(&gb->flip) ^ old) & 0x80000000u) == 0) {
+      if (ld_acquire(&gb->abort)) {
+        ok = 0;
+        break;
+      }
+      if (global_ns() - t0 > kBarrierLimitNs) {
+        atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
+        atomicExch(&gb->abort, 1u);
+        ok = 0;
+        break;
       }
     }
     if (ld_acquire(&gb->abort)) ok = 0;

@@ -54,19 +54,15 @@ struct Counters {
   unsigned int pad2;
 };
 
-// State of the grid-wide barrier of the persistent parallel kernel.
+// State of the grid-wide barriers of the persistent parallel kernels (one
+// arrival atomic per block: every block adds 1 but block 0, which adds
+// 2^31 - (blocks - 1), so the top bit of `flip` flips when the last block
+// arrives), and three counters (one per step mod 3) that the bounded-lanes
+// kernel's barrier sums a per-block count into on the way.
 struct GridBarrier {
-  unsigned int count;  // leaf arrivals at the root in the current generation
-  unsigned int gen;    // generation the waiting blocks watch
-  unsigned int abort;  // set by a block that gave up waiting
-  unsigned int pad[29];
-  unsigned int leaf[16 * 32];  // block arrivals per leaf, one 128-byte line each
-  // A second barrier, one arrival atomic per block: every block adds 1 but
-  // block 0, which adds 2^31 - (blocks - 1), so the top bit flips when the
-  // last block arrives; and three counters (one per step mod 3) summing a
-  // per-block count on the way.
   unsigned int flip;
-  unsigned int pad3[31];
+  unsigned int abort;  // set by a thread that gave up waiting
+  unsigned int pad[30];
   unsigned int sums[3 * 32];  // one 128-byte line each
 };
 
