@@ -158,6 +158,17 @@ int swe_world_device_field(swe_world* w, swe_field f, void** dev_ptr);
  * numbers lives on the device). */
 int swe_world_erode(swe_world* w, int cycles, int particles_per_cycle, swe_mode mode);
 
+/* The PARALLEL mode's cycle counter: the number of parallel erode cycles
+ * the world has run, which keys its random numbers together with the seed.
+ * A checkpoint is the nine fields (swe_world_download), the seed and this
+ * counter; a world created with the same seed and parameters, given the
+ * fields (swe_world_upload) and the counter, continues exactly as the
+ * original would. (The reference has no checkpointing; its ORDERED-mode
+ * counterpart is the C library rand() state, which a caller can replay with
+ * swe_world_seed_rand plus a rand tape.) The getter waits for the stream. */
+int swe_world_get_cycle(swe_world* w, uint64_t* cycle);
+int swe_world_set_cycle(swe_world* w, uint64_t cycle);
+
 /* An ensemble: `cycles` PARALLEL erode cycles of worlds[i] with
  * particles_per_cycle[i] particles each, for `count` independent worlds
  * (sizes, seeds, winds and parameters of their own). Each world's result is

@@ -134,6 +134,8 @@ def _setup(L):
     L.swe_world_terrain.argtypes = [_P, ctypes.POINTER(_CTerrain)]
     L.swe_terrain_default.argtypes = [ctypes.POINTER(_CTerrain)]
     L.swe_terrain_default.restype = None
+    L.swe_world_get_cycle.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
+    L.swe_world_set_cycle.argtypes = [_P, ctypes.c_uint64]
     L.swe_batch_erode.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.swe_world_sync.argtypes = [_P]
     L.swe_world_status.argtypes = [_P, ctypes.POINTER(ctypes.c_uint32)]
@@ -358,6 +360,17 @@ class World:
         out = np.empty(self.n * 3, dtype=np.float32)
         _check(lib.swe_world_normals(self._h, _ptr(out), out.size))
         return out.reshape(self.nx, self.nz, 3)
+
+    @property
+    def cycle(self) -> int:
+        """PARALLEL-mode cycle counter (keys the random numbers with the seed)."""
+        v = ctypes.c_uint64()
+        _check(lib.swe_world_get_cycle(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    @cycle.setter
+    def cycle(self, value: int) -> None:
+        _check(lib.swe_world_set_cycle(self._h, ctypes.c_uint64(int(value))))
 
     def vertices(self) -> np.ndarray:
         """swe_world_vertices: [nx, nz, 12] floats per cell, the position,

@@ -425,6 +425,25 @@ int swe_world_erode(swe_world* w, int cycles, int particles, swe_mode mode) {
   return SWE_OK;
 }
 
+int swe_world_get_cycle(swe_world* w, uint64_t* cycle) {
+  if (!w || !cycle) return fail(SWE_ERR_INVALID, "NULL argument");
+  if (int rc = use_device(w)) return rc;
+  unsigned long long v = 0;
+  SWE_CK(cudaMemcpyAsync(&v, &w->cnt->cycle, sizeof(v), cudaMemcpyDeviceToHost, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  *cycle = v;
+  return SWE_OK;
+}
+
+int swe_world_set_cycle(swe_world* w, uint64_t cycle) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (int rc = use_device(w)) return rc;
+  const unsigned long long v = cycle;
+  SWE_CK(cudaMemcpyAsync(&w->cnt->cycle, &v, sizeof(v), cudaMemcpyHostToDevice, w->stream));
+  SWE_CK(cudaStreamSynchronize(w->stream));
+  return SWE_OK;
+}
+
 int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle) {
   if (count < 0 || cycles < 0) return fail(SWE_ERR_INVALID, "count and cycles must be >= 0");
   if (count == 0) return SWE_OK;
