@@ -12,7 +12,8 @@ and, with --vertices, vertices.npy (updatenode's per-cell position, normal
 and edges).
 
     python -m simplewinderosion_gb300.cli [SEED] [--size 512] [--frames 10]
-        [--mode parallel|ordered] [--terrain bump|fbm] [--export DIR] [--every 1]
+        [--mode parallel|ordered] [--terrain bump|fbm] [--wind X,Y,Z]
+        [--export DIR] [--every 1]
 """
 from __future__ import annotations
 
@@ -32,6 +33,8 @@ def parse_args(argv=None):
     ap.add_argument("--frames", type=int, default=10, help="frames to run")
     ap.add_argument("--mode", choices=["parallel", "ordered"], default="parallel")
     ap.add_argument("--lanes", type=int, default=0, help="parallel mode: particles in flight (0: default)")
+    ap.add_argument("--wind", type=str, default=None,
+                    help="prevailing wind X,Y,Z, normalised (default: the reference's Wind::pspeed, 1,0,0)")
     ap.add_argument("--terrain", choices=["bump", "fbm"], default="bump",
                     help="bump: the reference's map::init terrain; fbm: seeded fBm plus a sediment layer")
     ap.add_argument("--export", type=Path, default=None, help="directory for the observables")
@@ -41,6 +44,14 @@ def parse_args(argv=None):
     args = ap.parse_args(argv)
     if args.size < 1 or args.frames < 0 or args.every < 1:
         ap.error("size >= 1, frames >= 0 and every >= 1 are required")
+    if args.wind is not None:
+        try:
+            w = [float(v) for v in args.wind.split(",")]
+        except ValueError:
+            w = []
+        if len(w) != 3 or not any(w):
+            ap.error("--wind takes three numbers X,Y,Z, not all zero")
+        args.wind = tuple(w)
     return args
 
 
@@ -73,7 +84,10 @@ def main(argv=None) -> int:
     seed = args.seed if args.seed is not None else int(time.time())
     particles = args.particles or 8 * args.size
     mode = swe.Mode.PARALLEL if args.mode == "parallel" else swe.Mode.ORDERED
-    world = swe.World(args.size, params=swe.Params(lanes=args.lanes), seed=seed)
+    params = swe.Params(lanes=args.lanes)
+    if args.wind is not None:
+        params = swe.Params(lanes=args.lanes, pspeed=swe.wind_direction(*args.wind))
+    world = swe.World(args.size, params=params, seed=seed)
     try:
         if args.terrain == "bump":
             world.terrain()

@@ -13,6 +13,10 @@ def test_defaults_are_the_app_cadence():
     assert a.seed == 42 and a.size == 64 and a.frames == 2
     with pytest.raises(SystemExit):
         cli.parse_args(["--every", "0"])
+    assert cli.parse_args(["--wind", "1,0,1"]).wind == (1.0, 0.0, 1.0)
+    for bad in ["1,0", "0,0,0", "a,b,c"]:
+        with pytest.raises(SystemExit):
+            cli.parse_args(["--wind", bad])
 
 
 def test_ppm_writer(tmp_path):
@@ -31,7 +35,7 @@ def test_ppm_writer(tmp_path):
 @pytest.mark.parametrize("mode,terrain", [("parallel", "bump"), ("ordered", "fbm")])
 def test_run_and_export(tmp_path, mode, terrain):
     rc = cli.main(["7", "--size", "64", "--frames", "3", "--every", "2", "--export", str(tmp_path),
-                   "--vertices", "--quiet", "--mode", mode, "--terrain", terrain])
+                   "--vertices", "--quiet", "--mode", mode, "--terrain", terrain, "--wind", "1,0,1"])
     assert rc == 0
     d = tmp_path / "frame_000001"
     h = np.load(d / "height.npy")
