@@ -98,7 +98,7 @@ struct swe_world {
   // parallel mode
   int32_t* hq = nullptr;      // heights; deltas, visit counts, owners of even and odd steps; 3 visited bitmaps
   long long* tq = nullptr;    // 4n
-  unsigned long long* hw = nullptr;  // n height words of the cluster form
+  unsigned long long* hw = nullptr;  // n height words of the bounded-lanes form, one padding word each side
   void* pstate = nullptr;     // 2 buffers x 9 arrays x capacity
   int pcap = 0;
   swe::ParallelBuffers pb{};
@@ -147,7 +147,7 @@ int ensure_parallel(swe_world* w, int particles) {
     SWE_CK(cudaMalloc(&w->hq, sizeof(int32_t) * (7 * stride + 3 * bw)));
     SWE_CK(cudaMemsetAsync(w->hq, 0, sizeof(int32_t) * (7 * stride + 3 * bw), w->stream));
     SWE_CK(cudaMalloc(&w->tq, sizeof(long long) * 4 * w->n));
-    SWE_CK(cudaMalloc(&w->hw, sizeof(unsigned long long) * w->n));
+    SWE_CK(cudaMalloc(&w->hw, sizeof(unsigned long long) * (w->n + 2)));
     SWE_CK(cudaMemsetAsync(w->tq, 0, sizeof(long long) * 4 * w->n, w->stream));
     SWE_CK(cudaMalloc(&w->dsum, sizeof(long long)));
     SWE_CK(cudaMalloc(&w->gbar, sizeof(swe::GridBarrier)));
@@ -172,7 +172,7 @@ int ensure_parallel(swe_world* w, int particles) {
   B.owner2 = w->hq + 6 * stride;
   for (int k = 0; k < 3; k++) B.vbits[k] = reinterpret_cast<uint32_t*>(w->hq + 7 * stride + k * bw);
   B.vbits_words = (long)((w->n + 128) / 32 + 2);
-  B.hw = w->hw;
+  B.hw = w->hw + 1;
   for (int k = 0; k < 4; k++) B.tq[k] = w->tq + (size_t)k * w->n;
   int32_t* base = reinterpret_cast<int32_t*>(w->pstate);
   for (int b = 0; b < 2; b++) {

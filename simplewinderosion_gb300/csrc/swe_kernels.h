@@ -45,7 +45,7 @@ struct ParallelBuffers {
   int32_t* owner2;
   uint32_t* vbits[3];  // visited bitmaps of steps 0, 1, 2 mod 3 (cell i: bit 64 + i)
   long vbits_words;    // words in each bitmap, (n + 128) / 32 + 2
-  unsigned long long* hw;  // height words (fixed-point height, write tag)
+  unsigned long long* hw;  // height words (fixed-point height, write tag); hw[-1] and hw[n] exist (padding)
   long long* tq[4];    // track accumulators (massflow, momx, momy, momz), 2^-32 units
   ParticleSoA state[2];
   int capacity;        // particles the state buffers hold

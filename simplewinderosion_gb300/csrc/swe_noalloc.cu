@@ -31,7 +31,7 @@ constexpr size_t kBitWords = ((kMaxCells + 128) / 32 + 2 + 63) & ~(size_t)63;  /
 // heights; deltas, owed cascades, owners of even and odd steps; 3 bitmaps
 constexpr size_t kMapsBytes = (7 * kMaxCells + 3 * kBitWords) * sizeof(int32_t);
 constexpr size_t kTracksBytes = 4 * kMaxCells * sizeof(long long);   // track accumulators
-constexpr size_t kWordsBytes = kMaxCells * sizeof(unsigned long long);  // height words
+constexpr size_t kWordsBytes = (kMaxCells + 32) * sizeof(unsigned long long);  // height words + padding
 constexpr size_t kParticleBytes = 2 * 9 * kMaxParticles * sizeof(int32_t);  // two state buffers
 constexpr size_t kScratchBytes =
     kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes + kWordsBytes + kParticleBytes;
@@ -130,7 +130,7 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   B.owner2 = maps + 6 * stride;
   for (int k = 0; k < 3; k++) B.vbits[k] = reinterpret_cast<uint32_t*>(maps + 7 * stride + k * kBitWords);
   B.vbits_words = (long)((n + 128) / 32 + 2);
-  B.hw = words;
+  B.hw = words + 1;  // one padding word before (and after) the map
   for (int k = 0; k < 4; k++) B.tq[k] = tracks + (size_t)k * n;
   for (int b = 0; b < 2; b++) {
     int32_t* q = pstate + (size_t)b * 9 * cap;

@@ -1219,10 +1219,13 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       const unsigned pbase = 16u * step;  // tag base of the previous step
       unsigned long long t_wait = 0;
       for (bool first = true;; first = false) {
-        unsigned long long wd[5];
+        // five loads every pass (rows off the map read the cell's own row;
+        // columns off the map land in the padding word or the next row)
+        unsigned long long wd[5] = {0, 0, 0, 0, 0};
+        if (ci >= 0) {
 #pragma unroll
-        for (int q = 0; q < 5; q++)
-          wd[q] = (((need & ~ready) >> q) & 1u) ? ld_relaxed64(HW + ci + nbr[q]) : 0ull;
+          for (int q = 0; q < 5; q++) wd[q] = ld_relaxed64(HW + ci + ((need >> q) & 1u ? nbr[q] : 0));
+        }
         if (first && check && ci >= 0) {
           prev = pb.bits() & inm;
 #pragma unroll
@@ -1359,6 +1362,9 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       unsigned visited = 0, lower = 0, ready = 0, okmask = 0, inmask = 0;
       unsigned long long wants = 0;  // 4 bits per word of the 3x3: the writes it must have had
       unsigned long long t_wait = 0;
+      // the 3x3 words by row (rows off the map point at the cell's own row,
+      // columns off the map land in the padding word or the next row)
+      unsigned long long* rp[3] = {HW, HW, HW};
       for (;;) {
         bool progressed = false;
         bool fresh = false;  // a new cell in hand: its visited bits were loaded in this pass
@@ -1396,6 +1402,9 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           for (int d = 0; d < 5; d++) inmask |= ((rows >> d) & 1u) ? cols << (5 * d) : 0u;
           // visited bits of the 5x5 block around (assembled below)
           cb.load(vb, x, z, nx, nz);
+          rp[1] = HW + ci - 1;
+          rp[0] = x > 0 ? rp[1] - nz : rp[1];
+          rp[2] = x + 1 < nx ? rp[1] + nz : rp[1];
           // the 3x3 neighbourhood's in-map cells (bit 3u+w)
           okmask = 0;
 #pragma unroll
@@ -1408,12 +1417,10 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         }
         // The words not taken yet, loaded in the same batch as the visited bits
         // (taken or off-map words read the cell's own word and are masked).
-        unsigned long long wd[9];
+        unsigned long long wd[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (cs >= 0) {
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-          const int u = q / 3, w = q % 3;
-          const bool need = cs >= 0 && (((okmask & ~ready) >> q) & 1u);
-          wd[q] = cs >= 0 ? ld_relaxed64(HW + (need ? ci + (u - 1) * nz + (w - 1) : ci)) : 0ull;
+          for (int q = 0; q < 9; q++) wd[q] = ld_relaxed64(rp[q / 3] + q % 3);
         }
         if (fresh) {
           // visited cells of the 5x5 block, and those of lower colour
@@ -1446,10 +1453,9 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
             // Every cell of the neighbourhood takes its next tag, changed or not.
 #pragma unroll
             for (int q = 0; q < 9; q++) {
-              const int u = q / 3, w = q % 3;
               if ((okmask >> q) & 1u) {
                 const unsigned want = (unsigned)(wants >> (4 * q)) & 15u;
-                st_relaxed64(HW + ci + (u - 1) * nz + (w - 1), make_word(N[q], tbase + want + 1));
+                st_relaxed64(rp[q / 3] + q % 3, make_word(N[q], tbase + want + 1));
               }
             }
             todo &= ~(1u << cs);
