@@ -45,6 +45,11 @@ def _pair(nx, nz, seed, wind=WIND_101, frac_bits=24, wseed=5, lanes=0):
     (50, 1, 200, 2, (1.0, 0.0, 0.0), 24, 0),
     (3, 2000, 6000, 1, (0.0, 0.0, 1.0), 16, 5000),
     (40, 40, 300, 1, WIND_101, 16, 1),
+    # a larger map through the cluster (default lanes) and the grid form, and
+    # the coarsest fixed-point format
+    (256, 256, 32768, 1, WIND_101, 16, 0),
+    (256, 256, 32768, 1, (0.0, 0.0, 1.0), 24, 8192),
+    (64, 64, 4096, 2, WIND_101, 8, 0),
 ])
 def test_parallel_bitwise_vs_cpu_model(nx, nz, particles, cycles, wind, frac_bits, lanes):
     port, w = _pair(nx, nz, 7, wind, frac_bits, lanes=lanes)
