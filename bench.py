@@ -61,9 +61,11 @@ def parse_args():
     ap.add_argument("--lanes", type=int, default=0,
                     help="particles in flight: 0 = default (cells/64, min 1024), -1 = all at once")
     ap.add_argument("--no-all-at-once", action="store_true")
-    ap.add_argument("--workload", choices=["plain1024", "ensemble"], default="plain1024",
-                    help="plain1024: the headline; ensemble: 64 terrains in one persistent launch")
+    ap.add_argument("--workload", choices=["plain1024", "ensemble", "exact-ensemble"], default="plain1024",
+                    help="plain1024: the headline; ensemble: 64 terrains in one persistent launch; "
+                         "exact-ensemble: independent 256^2 worlds in ORDERED mode, one thread each")
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
+    ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
     ap.add_argument("--cpu-sample", type=int, default=65536, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -556,12 +558,141 @@ def run_ensemble(args):
         w.close()
 
 
+def run_exact_ensemble(args):
+    """ORDERED mode at the reference's own small configuration, many times
+    over: `--worlds` independent 256^2 worlds (fBm of base frequency 1/64, 8
+    octaves, in [0, 0.5], plus 0.1 +- 0.02 sediment; wind normalize(1,0,1);
+    each world its own terrain and rand() seed), 1000 particles per cycle,
+    eroded by swe_batch_erode_ordered: every world bit for bit what the
+    reference's World::erode computes from its seed. One step = one cycle of
+    every world; the metric is aggregate particle-steps/s. The CPU baseline is
+    the oracle port (the same arithmetic) running one world's cycles on one
+    host core, the reference loop being single-threaded."""
+    import torch
+
+    import simplewinderosion_gb300 as swe
+    from oracle import oracle
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    torch.cuda.set_device(0)
+    size, particles = 256, 1000
+    wind = swe.wind_direction(1.0, 0.0, 1.0)
+    worlds = []
+    for k in range(args.worlds):
+        w = swe.World(size, params=swe.Params(pspeed=wind), seed=k + 1)
+        w.terrain(seed=k + 1, octaves=8, base_freq=1.0 / 64.0, sediment=0.1, sediment_jitter=0.02)
+        worlds.append(w)
+    h0 = worlds[0].height
+    stream = torch.cuda.ExternalStream(worlds[0].stream(), device=torch.device("cuda", 0))
+    for _ in range(args.warmup):
+        swe.batch_erode(worlds, 1, particles, mode=swe.Mode.ORDERED)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    total_ms, psteps, transfers = 0.0, 0, 0
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        swe.batch_erode(worlds, 1, particles, mode=swe.Mode.ORDERED)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        st = [w.stats() for w in worlds]
+        psteps += sum(x[0] for x in st)
+        transfers += sum(x[2] for x in st)
+    clocks = sampler.stop()
+    value = psteps / (total_ms / 1e3)
+    ms_per_step = total_ms / args.steps
+
+    # Algorithmic bytes per particle-step: the 3x3 height gather 36, four
+    # track read-modify-writes 32, the cell's height write 4, 4 per cascade
+    # transfer.
+    k = transfers / max(psteps, 1)
+    bytes_per_step = 72.0 + 4.0 * k
+    achieved = bytes_per_step * value / 1e9
+    peak, peak_note = FALLBACK_HBM_GBS, "fallback"
+    try:
+        peak = float(json.loads(PEAKS_FILE.read_text())["hbm_gbs"])
+        peak_note = "measured"
+    except Exception:
+        pass
+
+    # e2e: every world's height map kept on the host (pinned), uploaded and
+    # read back around each cycle through the C ABI.
+    n = size * size
+    host = torch.empty((args.worlds, n), dtype=torch.float32).pin_memory()
+    for i, w in enumerate(worlds):
+        w.download_ptr(swe.Field.HEIGHT, host[i].data_ptr(), n)
+    e2e_ms, e2e_steps = 0.0, 0
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i, w in enumerate(worlds):
+            w.upload_ptr(swe.Field.HEIGHT, host[i].data_ptr(), n)
+        swe.batch_erode(worlds, 1, particles, mode=swe.Mode.ORDERED)
+        for i, w in enumerate(worlds):
+            w.download_ptr(swe.Field.HEIGHT, host[i].data_ptr(), n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        e2e_steps += sum(w.stats()[0] for w in worlds)
+
+    # CPU baseline: one whole run of the configuration (100 cycles) on world
+    # 0's initial terrain, on one core.
+    port = oracle.Port(size, pspeed=wind)
+    port.set_field(0, h0)
+    port.seed(1)
+    t0 = time.perf_counter()
+    port.erode(particles, 100)
+    cpu_s = time.perf_counter() - t0
+    cpu_value = port.stats()[0] / cpu_s
+
+    line = {
+        "metric": "aggregate particle-steps/s, ORDERED-mode ensemble (each world bit-identical to the reference)",
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{args.worlds} worlds of 256^2, fBm(1/64)+sediment, wind normalize(1,0,1), "
+                               f"1000 particles per cycle, ORDERED mode",
+                   "worlds": args.worlds, "particles_per_cycle": particles,
+                   "l2": f"working set {args.worlds * 9 * n * 4 / 2**30:.1f} GiB, larger than L2",
+                   "reference_runs_per_s": args.worlds / (ms_per_step / 1e3) / 100.0},
+        "roofline": {"bound": "hbm", "kernel": "k_ordered_batch (one thread per world)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_note,
+                     "bytes_per_particle_step": bytes_per_step, "traffic": None},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+        "e2e": {"value": e2e_steps / (e2e_ms / 1e3), "unit": "particle-steps/s",
+                "h2d_bytes_per_step": 4 * n * args.worlds, "d2h_bytes_per_step": 4 * n * args.worlds},
+        "cpu_baseline": {"value": cpu_value, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                         "sample": f"one run (100 cycles x 1000 particles) of world 0 on {cpu_cores_desc()}, "
+                                   f"one thread ({cpu_s:.1f} s)"},
+    }
+    print(json.dumps(line), flush=True)
+    for w in worlds:
+        w.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
+    elif args.workload == "exact-ensemble":
+        run_exact_ensemble(args)
     else:
         run_ours(args)
 

@@ -182,6 +182,20 @@ int swe_world_set_cycle(swe_world* w, uint64_t cycle);
  * world (world.hpp:36-77). */
 int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle);
 
+/* An ensemble in ORDERED mode: `cycles` erode cycles of worlds[i] with
+ * particles_per_cycle[i] particles each, every world bit for bit what
+ * swe_world_erode(worlds[i], cycles, particles_per_cycle[i],
+ * SWE_MODE_ORDERED) gives, i.e. what the reference's World::erode
+ * (world.hpp:36-77) computes from that world's rand() state or rand tape.
+ * One world's particles are sequential, so each world runs on one GPU
+ * thread; the ensemble's throughput comes from running many worlds at once
+ * (one launch per cycle and sweep for all of them). All worlds must live on
+ * one device and be distinct. Runs on the first world's stream after the
+ * work queued on every world's stream, and returns after it has completed;
+ * device statuses (an exhausted rand tape) are reported per world by
+ * swe_world_sync. Extends the reference, which erodes one world. */
+int swe_batch_erode_ordered(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle);
+
 /* Wait for the world's queued work; returns SWE_ERR_DEVICE if a kernel set a
  * status bit since the last call (bits in *status if non-NULL, then cleared). */
 int swe_world_sync(swe_world* w);

@@ -137,6 +137,7 @@ def _setup(L):
     L.swe_world_get_cycle.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
     L.swe_world_set_cycle.argtypes = [_P, ctypes.c_uint64]
     L.swe_batch_erode.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.swe_batch_erode_ordered.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.swe_world_sync.argtypes = [_P]
     L.swe_world_status.argtypes = [_P, ctypes.POINTER(ctypes.c_uint32)]
     L.swe_world_seed_rand.argtypes = [_P, ctypes.c_uint32]
@@ -399,11 +400,13 @@ class World:
         _check(lib.swe_world_terrain(self._h, ctypes.byref(t)))
 
 
-def batch_erode(worlds, cycles: int, particles) -> None:
-    """swe_batch_erode: `cycles` PARALLEL erode cycles of every world of an
-    ensemble, particles[i] particles per cycle for worlds[i] (an int applies
-    to all). Each world ends as swe_world_erode would leave it; the worlds
-    that fit one 16-CTA cluster run together in one persistent launch."""
+def batch_erode(worlds, cycles: int, particles, mode: Mode = Mode.PARALLEL) -> None:
+    """`cycles` erode cycles of every world of an ensemble, particles[i]
+    particles per cycle for worlds[i] (an int applies to all). Each world
+    ends as swe_world_erode would leave it. PARALLEL (swe_batch_erode): the
+    worlds that fit one 16-CTA cluster run together in one persistent
+    launch. ORDERED (swe_batch_erode_ordered): every world bit for bit the
+    reference's sequential loop, one GPU thread per world."""
     worlds = list(worlds)
     if isinstance(particles, int):
         particles = [particles] * len(worlds)
@@ -411,4 +414,7 @@ def batch_erode(worlds, cycles: int, particles) -> None:
         raise ValueError("one particle count per world")
     handles = (_P * len(worlds))(*[w._h for w in worlds])
     counts = (ctypes.c_int * len(worlds))(*[int(p) for p in particles])
-    _check(lib.swe_batch_erode(handles, len(worlds), int(cycles), counts))
+    if Mode(mode) == Mode.ORDERED:
+        _check(lib.swe_batch_erode_ordered(handles, len(worlds), int(cycles), counts))
+    else:
+        _check(lib.swe_batch_erode(handles, len(worlds), int(cycles), counts))

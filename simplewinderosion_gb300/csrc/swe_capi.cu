@@ -505,6 +505,67 @@ int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* 
   return SWE_OK;
 }
 
+int swe_batch_erode_ordered(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle) {
+  if (count < 0 || cycles < 0) return fail(SWE_ERR_INVALID, "count and cycles must be >= 0");
+  if (count == 0) return SWE_OK;
+  if (!worlds || !particles_per_cycle) return fail(SWE_ERR_INVALID, "NULL argument");
+  for (int i = 0; i < count; i++) {
+    if (!worlds[i]) return fail(SWE_ERR_INVALID, "a world is NULL");
+    if (particles_per_cycle[i] < 0) return fail(SWE_ERR_INVALID, "particles_per_cycle must be >= 0");
+    if (worlds[i]->device != worlds[0]->device) return fail(SWE_ERR_INVALID, "worlds on different devices");
+  }
+  {
+    std::vector<swe_world*> sorted(worlds, worlds + count);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(SWE_ERR_INVALID, "a world appears twice in the batch");
+  }
+  if (int rc = use_device(worlds[0])) return rc;
+  // Everything runs on the first world's stream, after the work already
+  // queued on the others' streams.
+  cudaStream_t s = worlds[0]->stream;
+  for (int i = 1; i < count; i++) {
+    if (worlds[i]->stream == s) continue;
+    cudaEvent_t ev;
+    SWE_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, worlds[i]->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev, 0);
+    cudaEventDestroy(ev);
+    SWE_CK(e);
+  }
+  std::vector<swe::OrderedWorld> items(count);
+  long max_cells = 0;
+  for (int i = 0; i < count; i++) {
+    swe_world* w = worlds[i];
+    SWE_CK(cudaMemsetAsync(w->cnt, 0, 3 * sizeof(unsigned long long), s));
+    swe::OrderedWorld& o = items[i];
+    o.F = w->F;
+    o.c = w->consts();
+    o.rng = w->grand;
+    o.tape = w->tape;
+    o.tape_len = w->tape_len;
+    o.cnt = w->cnt;
+    o.n = w->n;
+    o.particles = particles_per_cycle[i];
+    if (w->n > max_cells) max_cells = w->n;
+  }
+  int rc = SWE_OK;
+  if (cycles > 0) {
+    int sms = 0;
+    SWE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, worlds[0]->device));
+    void* d = nullptr;
+    SWE_CK(cudaMallocAsync(&d, sizeof(swe::OrderedWorld) * count, s));
+    cudaError_t e = cudaMemcpyAsync(d, items.data(), sizeof(swe::OrderedWorld) * count, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = swe::launch_ordered_batch(static_cast<const swe::OrderedWorld*>(d), count, max_cells, cycles, sms, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = fail(SWE_ERR_CUDA, cudaGetErrorString(e));
+  }
+  for (int i = 0; i < count; i++) worlds[i]->hq_valid = false;
+  return rc;
+}
+
 int swe_world_status(swe_world* w, uint32_t* status) {
   if (!w) return fail(SWE_ERR_INVALID, "NULL world");
   if (int rc = use_device(w)) return rc;

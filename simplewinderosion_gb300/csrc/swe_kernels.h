@@ -23,6 +23,23 @@ void launch_reset_tracks(const Fields& F, long n, cudaStream_t s);
 void launch_ema_float(const Fields& F, float lrate, long n, cudaStream_t s);
 void launch_ordered_particles(const Fields& F, const Consts& c, GlibcRandState* rng, const int32_t* tape,
                               long long tape_len, Counters* cnt, int particles, cudaStream_t s);
+// One world of an ORDERED ensemble (launch_ordered_batch).
+struct OrderedWorld {
+  Fields F;
+  Consts c;
+  GlibcRandState* rng;
+  const int32_t* tape;  // nullptr: the rand() replica
+  long long tape_len;
+  Counters* cnt;
+  long n;         // cells
+  int particles;  // per cycle
+};
+// `cycles` ORDERED erode cycles of every world of the device array `worlds`
+// on stream s: per cycle all worlds' tracks are reset, each world's
+// particles run in order on one thread of its own, then the fields take
+// their update. max_cells: the largest world's cells; sms: the device's SMs.
+cudaError_t launch_ordered_batch(const OrderedWorld* worlds, int count, long max_cells, int cycles, int sms,
+                                 cudaStream_t s);
 void launch_trace(const float* height, const Consts& c, const float* spawn_xz, int n, int steps,
                   const int32_t* tape, float* out, cudaStream_t s);
 void launch_fly_live(const Fields& F, const Consts& c, float x, float z, int steps, const int32_t* tape,

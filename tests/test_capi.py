@@ -83,3 +83,6 @@ def test_batch_rejects_bad_arguments(lib_built):
     assert L.swe_batch_erode(None, -1, 1, None) == -1
     assert L.swe_batch_erode(None, 2, 1, None) == -1
     assert L.swe_batch_erode(None, 0, 1, None) == 0
+    assert L.swe_batch_erode_ordered(None, -1, 1, None) == -1
+    assert L.swe_batch_erode_ordered(None, 2, 1, None) == -1
+    assert L.swe_batch_erode_ordered(None, 0, 1, None) == 0
