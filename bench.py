@@ -66,6 +66,7 @@ def parse_args():
                          "exact-ensemble: independent 256^2 worlds in ORDERED mode, one thread each")
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
     ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
+    ap.add_argument("--exact-size", type=int, default=256, help="exact-ensemble: map side")
     ap.add_argument("--cpu-sample", type=int, default=65536, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -560,7 +561,7 @@ def run_ensemble(args):
 
 def run_exact_ensemble(args):
     """ORDERED mode at the reference's own small configuration, many times
-    over: `--worlds` independent 256^2 worlds (fBm of base frequency 1/64, 8
+    over: `--worlds` independent 256^2 worlds (`--exact-size`; fBm of base frequency 1/64, 8
     octaves, in [0, 0.5], plus 0.1 +- 0.02 sediment; wind normalize(1,0,1);
     each world its own terrain and rand() seed), 1000 particles per cycle,
     eroded by swe_batch_erode_ordered: every world bit for bit what the
@@ -577,7 +578,7 @@ def run_exact_ensemble(args):
     if rank != 0:
         return
     torch.cuda.set_device(0)
-    size, particles = 256, 1000
+    size, particles = args.exact_size, 1000
     wind = swe.wind_direction(1.0, 0.0, 1.0)
     worlds = []
     for k in range(args.worlds):
@@ -623,11 +624,11 @@ def run_exact_ensemble(args):
     # e2e: every world's height map kept on the host (pinned), uploaded and
     # read back around each cycle through the C ABI.
     n = size * size
-    host = torch.empty((args.worlds, n), dtype=torch.float32).pin_memory()
-    for i, w in enumerate(worlds):
-        w.download_ptr(swe.Field.HEIGHT, host[i].data_ptr(), n)
+    host = torch.empty((0 if args.no_e2e else args.worlds, n), dtype=torch.float32).pin_memory()
+    for i in range(host.shape[0]):
+        worlds[i].download_ptr(swe.Field.HEIGHT, host[i].data_ptr(), n)
     e2e_ms, e2e_steps = 0.0, 0
-    for _ in range(args.steps):
+    for _ in range(0 if args.no_e2e else args.steps):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -643,13 +644,17 @@ def run_exact_ensemble(args):
 
     # CPU baseline: one whole run of the configuration (100 cycles) on world
     # 0's initial terrain, on one core.
-    port = oracle.Port(size, pspeed=wind)
-    port.set_field(0, h0)
-    port.seed(1)
-    t0 = time.perf_counter()
-    port.erode(particles, 100)
-    cpu_s = time.perf_counter() - t0
-    cpu_value = port.stats()[0] / cpu_s
+    cpu = None
+    if not args.no_cpu_baseline:
+        port = oracle.Port(size, pspeed=wind)
+        port.set_field(0, h0)
+        port.seed(1)
+        t0 = time.perf_counter()
+        port.erode(particles, 100)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": port.stats()[0] / cpu_s, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": f"one run (100 cycles x 1000 particles) of world 0 on {cpu_cores_desc()}, "
+                         f"one thread ({cpu_s:.1f} s)"}
 
     line = {
         "metric": "aggregate particle-steps/s, ORDERED-mode ensemble (each world bit-identical to the reference)",
@@ -664,7 +669,7 @@ def run_exact_ensemble(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{args.worlds} worlds of 256^2, fBm(1/64)+sediment, wind normalize(1,0,1), "
+        "config": {"workload": f"{args.worlds} worlds of {size}^2, fBm(1/64)+sediment, wind normalize(1,0,1), "
                                f"1000 particles per cycle, ORDERED mode",
                    "worlds": args.worlds, "particles_per_cycle": particles,
                    "l2": f"working set {args.worlds * 9 * n * 4 / 2**30:.1f} GiB, larger than L2",
@@ -674,12 +679,12 @@ def run_exact_ensemble(args):
                      "bytes_per_particle_step": bytes_per_step, "traffic": None},
         "gpu_launches": 3 * args.steps,
         "clocks": clocks,
-        "e2e": {"value": e2e_steps / (e2e_ms / 1e3), "unit": "particle-steps/s",
-                "h2d_bytes_per_step": 4 * n * args.worlds, "d2h_bytes_per_step": 4 * n * args.worlds},
-        "cpu_baseline": {"value": cpu_value, "unit": "particle-steps/s", "cores": 1, "kind": "port",
-                         "sample": f"one run (100 cycles x 1000 particles) of world 0 on {cpu_cores_desc()}, "
-                                   f"one thread ({cpu_s:.1f} s)"},
     }
+    if not args.no_e2e:
+        line["e2e"] = {"value": e2e_steps / (e2e_ms / 1e3), "unit": "particle-steps/s",
+                       "h2d_bytes_per_step": 4 * n * args.worlds, "d2h_bytes_per_step": 4 * n * args.worlds}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
     for w in worlds:
         w.close()
