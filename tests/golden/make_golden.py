@@ -72,6 +72,29 @@ def cascade_case(name, n, seed):
     np.savez_compressed(OUT / f"{name}.npz", height=h, cells=np.asarray(cells, np.int32), after=np.stack(after))
 
 
+def cascade_ties_case(name, n, seed):
+    """World::cascade on a map full of exact ties (quantised heights, +0 and
+    -0) with two NaN cells, at interior, edge and corner cells, next to the
+    NaNs and away from them."""
+    ref = oracle.Reference(n)
+    rs = np.random.RandomState(seed)
+    levels = np.asarray([0.0, -0.0, 0.05, 0.1, 0.1, 0.2], np.float32)
+    h = levels[rs.randint(0, len(levels), size=(n, n))].astype(np.float32)
+    h[4:7, 4:7] = 0.1                   # a plateau: eight equal neighbours
+    h[5, 5] = 0.3
+    h[9, 9] = np.float32(np.nan)        # interior NaN
+    h[0, 11] = np.float32(np.nan)       # edge NaN
+    ref.reset(h)
+    cells = [(5, 5), (4, 4), (8, 8), (9, 10), (10, 10), (1, 11), (0, 10), (0, 0), (n - 1, n - 1), (0, n - 1),
+             (5, 5), (12, 3), (9, 9)]
+    cells += [tuple(c) for c in rs.randint(0, n, size=(40, 2))]
+    after = []
+    for (x, z) in cells:
+        ref.cascade(int(x), int(z))
+        after.append(ref.get_field(0))
+    np.savez_compressed(OUT / f"{name}.npz", height=h, cells=np.asarray(cells, np.int32), after=np.stack(after))
+
+
 def trace_tape(seed, count, steps):
     """Raw rand()-like turbulence draws for frozen-map traces (regenerated
     from the seed by the tests; numpy's legacy RandomState stream is fixed)."""
@@ -113,6 +136,7 @@ def main():
     erode_case("erode_16_edges", 16, 13, 3, 60, 5, pspeed=(0.0, 0.0, -1.0))
     normals_case("normals_16", 16, 21)
     cascade_case("cascade_12", 16, 22)
+    cascade_ties_case("cascade_ties_nan", 16, 25)
     trace_case("trace_48_wind101", 48, 23, 32, 128, WIND_101)
     trace_case("trace_48_default", 48, 24, 32, 128, (1.0, 0.0, 0.0))
     for p in sorted(OUT.glob("*.npz")):

@@ -57,6 +57,22 @@ def test_golden_cascade():
         _check(after, port.get_field(0))
 
 
+def _same_with_nans(want, got):
+    # NaN payloads are the platform's; every other value bit for bit
+    assert np.array_equal(np.isnan(want), np.isnan(got))
+    m = ~np.isnan(want)
+    assert np.array_equal(bits(want[m]), bits(got[m]))
+
+
+def test_golden_cascade_ties_and_nans():
+    g = golden("cascade_ties_nan")
+    port = oracle.Port(16)
+    port.set_field(0, g["height"])
+    for (x, z), after in zip(g["cells"], g["after"]):
+        port.cascade(int(x), int(z))
+        _same_with_nans(after, port.get_field(0))
+
+
 def trace_tape(seed, count, steps):
     return np.random.RandomState(seed + 1000).randint(0, 2**31 - 1, size=(count, steps, 3)).astype(np.int32)
 

@@ -66,6 +66,38 @@ def test_cascade_golden_sequence():
         assert np.array_equal(bits(w.height), bits(after)), (x, z)
 
 
+def test_cascade_golden_ties_and_nans():
+    # equal heights (+0 and -0 among them) order by slot, as the reference's
+    # insertion sort leaves them; NaN neighbours take the step-by-step path
+    g = golden("cascade_ties_nan")
+    w = swe.World(16)
+    w.upload(swe.Field.HEIGHT, g["height"])
+    for (x, z), after in zip(g["cells"], g["after"]):
+        w.cascade(int(x), int(z))
+        got = w.height
+        assert np.array_equal(np.isnan(after), np.isnan(got)), (x, z)
+        m = ~np.isnan(after)
+        assert np.array_equal(bits(after[m]), bits(got[m])), (x, z)
+
+
+def test_ordered_on_plateaus_bitwise_vs_port():
+    # quantised heights: most cascades sort neighbours with equal heights
+    n = 48
+    rs = np.random.RandomState(31)
+    h = np.asarray([0.1, 0.1, 0.2, 0.0, -0.0], np.float32)[rs.randint(0, 5, (n, n))]
+    h[10:30, 10:30] = 0.15
+    port = oracle.Port(n, pspeed=WIND_101)
+    port.set_field(0, h)
+    port.seed(5)
+    port.erode(200, 2)
+    w = swe.World(n, params=swe.Params(pspeed=WIND_101), seed=5)
+    w.upload(swe.Field.HEIGHT, h)
+    w.erode(200, 2, mode=swe.Mode.ORDERED)
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), f
+    assert w.stats() == port.stats()
+
+
 def test_device_expf_equals_c_library_everywhere():
     # every float argument with a finite non-zero result: [-104, 0] and [0, 88.8]
     w = swe.World(8)
