@@ -29,6 +29,7 @@ struct FlyState {
   int age;
   float sediment;
   V3 pos, speed, pspeed;
+  V3 pdir;  // normalize(pspeed), which no step changes
 };
 
 // rand() replica of the C library (TYPE_3 additive feedback generator).
@@ -151,6 +152,20 @@ struct LiveMap {
   // then by slot, a total order whose sorted sequence is the stable one.
   // The transfers run branch-free along the sorted list.
   __device__ int cascade_interior(const Consts& c) {
+    // A cascade in which no neighbour moves against the current centre
+    // leaves the centre, hence every neighbour, unchanged, in any order:
+    // decide that first, without sorting.
+    {
+      const float md_side = sqrtf(1.0f) * c.maxdiff;
+      const float md_diag = sqrtf(2.0f) * c.maxdiff;
+      bool any = false;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const float diff = h[4] - h[nb_cell(k)];
+        any |= diff != 0.0f && !(fabsf(diff) - (((0xA5 >> k) & 1) ? md_diag : md_side) <= 0.0f);
+      }
+      if (!any) return 0;
+    }
     float ph[8];
     int pk[8];
 #pragma unroll
@@ -324,7 +339,7 @@ __device__ bool fly_exact(Map& m, const Consts& c, FlyState& P, Rand& rnd, int& 
   float hfac = exp_libm(-(P.pos.y - hc) / c.boundarylayer, c);
   if (hfac < 0.0f) hfac = 0.0f;
 
-  float shadow = dot(normalize(P.pspeed), n);
+  float shadow = dot(P.pdir, n);
   if (shadow < 0.0f) shadow = 0.0f;
   shadow = 1.0f - shadow;
   P.speed = add(P.speed, smul(0.05f, sub(smul(0.1f + 0.9f * shadow, P.pspeed), P.speed)));
@@ -372,6 +387,7 @@ __device__ __forceinline__ FlyState spawn_state(const Consts& c, float x, float 
   P.pos = v3(x, 0.0f, z);
   P.speed = v3(0.0f, 0.0f, 0.0f);
   P.pspeed = v3(c.px, c.py, c.pz);
+  P.pdir = normalize(P.pspeed);
   return P;
 }
 
