@@ -67,7 +67,7 @@ def parse_args():
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
     ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
     ap.add_argument("--exact-size", type=int, default=256, help="exact-ensemble: map side")
-    ap.add_argument("--cpu-sample", type=int, default=65536, help="particles in the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=196608, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
