@@ -314,6 +314,60 @@ int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, const swe_p
                                uint64_t first_cycle, int cycles, int particles_per_cycle, void* stream,
                                uint32_t* status);
 
+/* ---- Learned surrogate: building blocks of a BF16 U-Net ----
+ * No counterpart in the reference (an extension: a network that predicts
+ * the terrain after a number of erode cycles, trained on pairs the erosion
+ * path produces, with that path as its fallback and judge). Tensors are
+ * device arrays in NHWC order (channels innermost); "bf16" tensors hold
+ * bfloat16 values (uint16 storage) and must be 4-byte aligned; arithmetic
+ * accumulates in fp32. Every call is enqueued on `stream` (NULL: the default
+ * stream) and returns once enqueued.
+ *
+ * y[n,i,j,co] = bias[co] + sum over the 3x3 taps (zero padding) and ci of
+ * x[n,i+di,j+dj,ci] w[co,di+1,dj+1,ci]; x bf16 [n,h,w,cin], w bf16
+ * [cout,3,3,cin], bias fp32 [cout] or NULL, y bf16 [n,h,w,cout]; cin a
+ * multiple of 16, cout of 8. Runs on the tensor cores (implicit GEMM). */
+int swe_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int n, int h, int wd, int cin, int cout,
+                   void* stream);
+/* wf[ci,2-di,2-dj,co] = w[co,di,dj,ci]: the weights whose convolution of dy
+ * is the input gradient of swe_nn_conv3x3. */
+int swe_nn_conv3x3_flip(const void* w, void* wf, int cin, int cout, void* stream);
+/* Weight and bias gradients of swe_nn_conv3x3, ADDED to dw (fp32
+ * [cout,3,3,cin]) and db (fp32 [cout], or NULL) from its input x and the
+ * output gradient dy (bf16 [n,h,w,cout]). */
+int swe_nn_conv3x3_wgrad(const void* x, const void* dy, float* dw, float* db, int n, int h, int wd, int cin, int cout,
+                         void* stream);
+/* act = GELU(pre) = pre (1 + erf(pre / sqrt 2)) / 2, and dpre = dact GELU'(pre). */
+int swe_nn_gelu(const void* pre, void* act, int64_t count, void* stream);
+int swe_nn_gelu_bwd(const void* pre, const void* dact, void* dpre, int64_t count, void* stream);
+/* 2x2 average pooling of x [n,h,w,c] (h, w even) into y [n,h/2,w/2,c]; with
+ * backward != 0, x is the gradient [n,h/2,w/2,c] and y the input gradient
+ * [n,h,w,c]. */
+int swe_nn_pool2(const void* x, void* y, int n, int h, int wd, int c, int backward, void* stream);
+/* Nearest 2x upsampling of x [n,h,w,c] into y [n,2h,2w,c]; with backward !=
+ * 0, x is the gradient [n,2h,2w,c] and y the input gradient [n,h,w,c]. */
+int swe_nn_up2(const void* x, void* y, int n, int h, int wd, int c, int backward, void* stream);
+/* out = a + b (bf16, elementwise). */
+int swe_nn_add(const void* a, const void* b, void* out, int64_t count, void* stream);
+/* The network input, 16 bf16 channels per cell: (height - 0.25) * 4, the
+ * wind direction's x and z components (wind_xz: 2 floats per map), zeros.
+ * height fp32 [n,h,w]. */
+int swe_nn_pack_input(const float* height, const float* wind_xz, void* x, int n, int h, int wd, void* stream);
+/* Squared error of channel 0 of pred (bf16 [pixels, c]) against target *
+ * target_scale (target fp32 [pixels]): the sum of squares is ADDED to *loss
+ * (device fp32) and dpred = 2 (pred - target target_scale) grad_scale on
+ * channel 0, 0 on the others. */
+int swe_nn_mse(const void* pred, const float* target, float target_scale, void* dpred, float* loss, int64_t pixels,
+               int c, float grad_scale, void* stream);
+/* out[p] = channel 0 of pred (bf16 [pixels, c]) times out_scale, as fp32. */
+int swe_nn_channel0(const void* pred, float* out, int64_t pixels, int c, float out_scale, void* stream);
+/* One Adam step (step = 1, 2, ...) on fp32 weights w with gradient grad and
+ * moments m, v; w_bf16 (or NULL) receives the updated weights as bf16. */
+int swe_nn_adam(float* w, const float* grad, float* m, float* v, void* w_bf16, int64_t count, float lr, float beta1,
+                float beta2, float eps, int step, void* stream);
+/* b = bf16(a). */
+int swe_nn_to_bf16(const float* a, void* b, int64_t count, void* stream);
+
 /* Message of the calling thread's last error ("" if none). */
 const char* swe_last_error(void);
 

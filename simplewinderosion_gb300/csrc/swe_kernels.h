@@ -117,4 +117,23 @@ bool batch_fits(int lanes, int nx, int nz);
 // point). Returns after the launch has completed.
 cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s);
 
+// ---- learned surrogate building blocks (swe_surrogate.cu): bf16 NHWC ----
+cudaError_t nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int N, int H, int W, int cin,
+                       int cout, cudaStream_t s);
+cudaError_t nn_flip(const void* w, void* wf, int cin, int cout, cudaStream_t s);
+cudaError_t nn_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int N, int H, int W, int cin, int cout,
+                          cudaStream_t s);
+cudaError_t nn_gelu(const void* pre, void* act, long n, cudaStream_t s);
+cudaError_t nn_gelu_bwd(const void* pre, const void* dact, void* dpre, long n, cudaStream_t s);
+cudaError_t nn_pool2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s);
+cudaError_t nn_up2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s);
+cudaError_t nn_add(const void* a, const void* b, void* out, long n, cudaStream_t s);
+cudaError_t nn_pack_input(const float* h, const float* wind_xz, void* x, int N, int H, int W, cudaStream_t s);
+cudaError_t nn_mse(const void* pred, const float* target, float tscale, void* dpred, float* loss, long M, int C,
+                   float gscale, cudaStream_t s);
+cudaError_t nn_channel0(const void* pred, float* out, long M, int C, float oscale, cudaStream_t s);
+cudaError_t nn_adam(float* w, const float* grad, float* m, float* v, void* w16, long n, float lr, float b1, float b2,
+                    float eps, int step, cudaStream_t s);
+cudaError_t nn_to_bf16(const float* a, void* b, long n, cudaStream_t s);
+
 }  // namespace swe

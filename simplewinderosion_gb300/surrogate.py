@@ -1,0 +1,364 @@
+"""Learned surrogate: a BF16 U-Net that predicts the height change of a
+terrain after a fixed number of erode cycles.
+
+The network (channels 32/64/96/128 over four levels, 3x3 convolutions, GELU,
+2x2 average pooling, nearest 2x upsampling, additive skips) runs on the
+library's own kernels (csrc/swe_surrogate.cu, through the C ABI in
+include/swe.h): tensor-core implicit-GEMM convolutions with fp32
+accumulation, BF16 weights and activations, fp32 master weights and Adam.
+Torch provides device memory and the stream only.
+
+Training pairs come from the erosion path itself (`make_pairs`: ensembles of
+seeded fBm terrains with random winds, eroded by swe_batch_erode in PARALLEL
+mode, the plain GPU method), and the erosion path stays the judge: `Rollout` advances a terrain by
+predicted jumps and, every `judge_every` jumps, runs the plain method over
+the same jump and rejects the surrogate (falling back to the plain method)
+once a prediction's height RMSE exceeds the bound.
+
+Input: 16 channels per cell (height, the wind direction's x and z, zeros);
+output channel 0 is the height change times `Surrogate.scale`. Map sides
+must be multiples of 8.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import Field, Mode, Params, World, batch_erode, lib, wind_direction, _check
+
+# (name, cin, cout) in forward order
+LAYERS = [("in", 16, 32), ("e0", 32, 32), ("d1", 32, 64), ("d2", 64, 96), ("d3", 96, 128), ("b3", 128, 128),
+          ("u2", 128, 96), ("u1", 96, 64), ("u0", 64, 32), ("out", 32, 16)]
+
+_P = ctypes.c_void_p
+_bound = False
+
+
+def _bind():
+    global _bound
+    if _bound:
+        return
+    L = lib
+    i64, f32, i32 = ctypes.c_int64, ctypes.c_float, ctypes.c_int
+    L.swe_nn_conv3x3.argtypes = [_P, _P, _P, _P, i32, i32, i32, i32, i32, _P]
+    L.swe_nn_conv3x3_flip.argtypes = [_P, _P, i32, i32, _P]
+    L.swe_nn_conv3x3_wgrad.argtypes = [_P, _P, _P, _P, i32, i32, i32, i32, i32, _P]
+    L.swe_nn_gelu.argtypes = [_P, _P, i64, _P]
+    L.swe_nn_gelu_bwd.argtypes = [_P, _P, _P, i64, _P]
+    L.swe_nn_pool2.argtypes = [_P, _P, i32, i32, i32, i32, i32, _P]
+    L.swe_nn_up2.argtypes = [_P, _P, i32, i32, i32, i32, i32, _P]
+    L.swe_nn_add.argtypes = [_P, _P, _P, i64, _P]
+    L.swe_nn_pack_input.argtypes = [_P, _P, _P, i32, i32, i32, _P]
+    L.swe_nn_mse.argtypes = [_P, _P, f32, _P, _P, i64, i32, f32, _P]
+    L.swe_nn_channel0.argtypes = [_P, _P, i64, i32, f32, _P]
+    L.swe_nn_adam.argtypes = [_P, _P, _P, _P, _P, i64, f32, f32, f32, f32, i32, _P]
+    L.swe_nn_to_bf16.argtypes = [_P, _P, i64, _P]
+    _bound = True
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class Ops:
+    """The building blocks on torch tensors (bf16 NHWC activations)."""
+
+    def __init__(self, torch, device):
+        _bind()
+        self.torch = torch
+        self.device = device
+
+    @property
+    def s(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream(self.device).cuda_stream)
+
+    def empty(self, *shape, dtype=None):
+        return self.torch.empty(shape, dtype=dtype or self.torch.bfloat16, device=self.device)
+
+    def conv(self, x, w16, b, cout):
+        n, h, wd, cin = x.shape
+        y = self.empty(n, h, wd, cout)
+        _check(lib.swe_nn_conv3x3(_p(x), _p(w16), _p(b), _p(y), n, h, wd, cin, cout, self.s))
+        return y
+
+    def conv_dx(self, dy, w16, cin):
+        n, h, wd, cout = dy.shape
+        wf = self.empty(cin, 3, 3, cout)
+        _check(lib.swe_nn_conv3x3_flip(_p(w16), _p(wf), cin, cout, self.s))
+        dx = self.empty(n, h, wd, cin)
+        _check(lib.swe_nn_conv3x3(_p(dy), _p(wf), None, _p(dx), n, h, wd, cout, cin, self.s))
+        return dx
+
+    def wgrad(self, x, dy, dw, db):
+        n, h, wd, cin = x.shape
+        _check(lib.swe_nn_conv3x3_wgrad(_p(x), _p(dy), _p(dw), _p(db), n, h, wd, cin, dy.shape[3], self.s))
+
+    def gelu(self, pre):
+        y = self.empty(*pre.shape)
+        _check(lib.swe_nn_gelu(_p(pre), _p(y), pre.numel(), self.s))
+        return y
+
+    def gelu_bwd(self, pre, dact):
+        y = self.empty(*pre.shape)
+        _check(lib.swe_nn_gelu_bwd(_p(pre), _p(dact), _p(y), pre.numel(), self.s))
+        return y
+
+    def pool(self, x):
+        n, h, wd, c = x.shape
+        y = self.empty(n, h // 2, wd // 2, c)
+        _check(lib.swe_nn_pool2(_p(x), _p(y), n, h, wd, c, 0, self.s))
+        return y
+
+    def pool_bwd(self, dy):
+        n, h, wd, c = dy.shape
+        dx = self.empty(n, 2 * h, 2 * wd, c)
+        _check(lib.swe_nn_pool2(_p(dy), _p(dx), n, 2 * h, 2 * wd, c, 1, self.s))
+        return dx
+
+    def up(self, x):
+        n, h, wd, c = x.shape
+        y = self.empty(n, 2 * h, 2 * wd, c)
+        _check(lib.swe_nn_up2(_p(x), _p(y), n, h, wd, c, 0, self.s))
+        return y
+
+    def up_bwd(self, dy):
+        n, h, wd, c = dy.shape
+        dx = self.empty(n, h // 2, wd // 2, c)
+        _check(lib.swe_nn_up2(_p(dy), _p(dx), n, h // 2, wd // 2, c, 1, self.s))
+        return dx
+
+    def add(self, a, b):
+        y = self.empty(*a.shape)
+        _check(lib.swe_nn_add(_p(a), _p(b), _p(y), a.numel(), self.s))
+        return y
+
+    def pack(self, height, wind_xz):
+        n, h, wd = height.shape
+        x = self.empty(n, h, wd, 16)
+        _check(lib.swe_nn_pack_input(_p(height), _p(wind_xz), _p(x), n, h, wd, self.s))
+        return x
+
+
+class Surrogate:
+    """The U-Net, its fp32 master weights, bf16 copies, gradients and Adam
+    moments. `scale`: the height change is predicted as change * scale."""
+
+    def __init__(self, device="cuda", seed=0, scale=100.0):
+        import torch
+        self.torch = torch
+        self.device = torch.device(device)
+        self.ops = Ops(torch, self.device)
+        self.scale = float(scale)
+        rs = np.random.RandomState(seed)
+        self.w, self.b, self.w16 = {}, {}, {}
+        for name, cin, cout in LAYERS:
+            fan_in = 9 * (3 if name == "in" else cin)
+            std = math.sqrt(2.0 / fan_in) * (0.1 if name == "out" else 1.0)
+            w = (rs.standard_normal((cout, 3, 3, cin)) * std).astype(np.float32)
+            if name == "in":
+                w[..., 3:] = 0.0  # the padding channels carry zeros
+            self.w[name] = torch.from_numpy(w).to(self.device)
+            self.b[name] = torch.zeros(cout, dtype=torch.float32, device=self.device)
+        self.gw = {k: torch.zeros_like(v) for k, v in self.w.items()}
+        self.gb = {k: torch.zeros_like(v) for k, v in self.b.items()}
+        self.m = {k: torch.zeros_like(v) for k, v in list(self.w.items())}
+        self.v = {k: torch.zeros_like(v) for k, v in list(self.w.items())}
+        self.mb = {k: torch.zeros_like(v) for k, v in self.b.items()}
+        self.vb = {k: torch.zeros_like(v) for k, v in self.b.items()}
+        self.t = 0
+        self.sync_bf16()
+
+    def sync_bf16(self):
+        for k, w in self.w.items():
+            if k not in self.w16:
+                self.w16[k] = self.ops.empty(*w.shape)
+            _check(lib.swe_nn_to_bf16(_p(w), _p(self.w16[k]), w.numel(), self.ops.s))
+
+    def state(self) -> dict:
+        out = {"scale": np.float32(self.scale)}
+        for k in self.w:
+            out[f"w_{k}"] = self.w[k].cpu().numpy()
+            out[f"b_{k}"] = self.b[k].cpu().numpy()
+        return out
+
+    def load(self, state: dict):
+        self.scale = float(state["scale"])
+        for k in self.w:
+            self.w[k].copy_(self.torch.from_numpy(np.asarray(state[f"w_{k}"], np.float32)))
+            self.b[k].copy_(self.torch.from_numpy(np.asarray(state[f"b_{k}"], np.float32)))
+        self.sync_bf16()
+
+    # ---- forward / backward ----
+    def forward(self, x):
+        """x: bf16 [n,h,w,16]. Returns the output tensor [n,h,w,16] and the
+        cache of the backward pass."""
+        o = self.ops
+        cache = {}
+
+        def conv_act(name, inp):
+            pre = o.conv(inp, self.w16[name], self.b[name], self.b[name].numel())
+            cache[name] = (inp, pre)
+            return o.gelu(pre)
+
+        a_in = conv_act("in", x)
+        s0 = conv_act("e0", a_in)
+        s1 = conv_act("d1", o.pool(s0))
+        s2 = conv_act("d2", o.pool(s1))
+        s3 = conv_act("d3", o.pool(s2))
+        b3 = conv_act("b3", s3)
+        d2 = o.add(conv_act("u2", o.up(b3)), s2)
+        d1 = o.add(conv_act("u1", o.up(d2)), s1)
+        d0 = o.add(conv_act("u0", o.up(d1)), s0)
+        out = o.conv(d0, self.w16["out"], self.b["out"], 16)
+        cache["out"] = (d0, out)
+        return out, cache
+
+    def backward(self, cache, dout):
+        """Adds the gradients of every weight and bias from d loss / d out."""
+        o = self.ops
+        d0, _ = cache["out"]
+        o.wgrad(d0, dout, self.gw["out"], self.gb["out"])
+        dd0 = o.conv_dx(dout, self.w16["out"], 32)
+
+        def back(name, dact):
+            inp, pre = cache[name]
+            dpre = o.gelu_bwd(pre, dact)
+            o.wgrad(inp, dpre, self.gw[name], self.gb[name])
+            return o.conv_dx(dpre, self.w16[name], inp.shape[3]) if name != "in" else None
+
+        dd1 = o.up_bwd(back("u0", dd0))
+        dd2 = o.up_bwd(back("u1", dd1))
+        db3 = o.up_bwd(back("u2", dd2))
+        ds3 = back("b3", db3)
+        ds2 = o.add(dd2, o.pool_bwd(back("d3", ds3)))
+        ds1 = o.add(dd1, o.pool_bwd(back("d2", ds2)))
+        ds0 = o.add(dd0, o.pool_bwd(back("d1", ds1)))
+        da_in = back("e0", ds0)
+        back("in", da_in)
+
+    def zero_grad(self):
+        for k in self.gw:
+            self.gw[k].zero_()
+            self.gb[k].zero_()
+
+    def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.t += 1
+        s = self.ops.s
+        for k in self.w:
+            _check(lib.swe_nn_adam(_p(self.w[k]), _p(self.gw[k]), _p(self.m[k]), _p(self.v[k]), _p(self.w16[k]),
+                                   self.w[k].numel(), lr, b1, b2, eps, self.t, s))
+            _check(lib.swe_nn_adam(_p(self.b[k]), _p(self.gb[k]), _p(self.mb[k]), _p(self.vb[k]), None,
+                                   self.b[k].numel(), lr, b1, b2, eps, self.t, s))
+
+    # ---- training and prediction ----
+    def train_step(self, height, wind_xz, target_dh, lr=1e-3):
+        """One Adam step on a batch: height fp32 [n,h,w], wind_xz fp32 [n,2],
+        target_dh fp32 [n,h,w] (unscaled). Returns the mean squared error of
+        the scaled prediction."""
+        torch = self.torch
+        x = self.ops.pack(height, wind_xz)
+        out, cache = self.forward(x)
+        dout = self.ops.empty(*out.shape)
+        loss = torch.zeros(1, dtype=torch.float32, device=self.device)
+        m = out.shape[0] * out.shape[1] * out.shape[2]
+        _check(lib.swe_nn_mse(_p(out), _p(target_dh), self.scale, _p(dout), _p(loss), m, 16, 1.0 / m, self.ops.s))
+        self.zero_grad()
+        self.backward(cache, dout)
+        self.adam(lr)
+        return float(loss.item()) / m
+
+    def predict(self, height, wind_xz):
+        """Predicted height change, fp32 [n,h,w]."""
+        torch = self.torch
+        x = self.ops.pack(height, wind_xz)
+        out, _ = self.forward(x)
+        n, h, wd, _ = out.shape
+        ch0 = torch.empty((n, h, wd), dtype=torch.float32, device=self.device)
+        _check(lib.swe_nn_channel0(_p(out), _p(ch0), n * h * wd, 16, 1.0 / self.scale, self.ops.s))
+        return ch0
+
+
+def make_pairs(count, size=256, cycles=50, particles=1000, seed=0, chunk=2048, mode=Mode.PARALLEL):
+    """Training pairs from the erosion path: `count` seeded fBm terrains
+    (8 octaves, base frequency 1/64, persistence uniform in [0.4, 0.6], in
+    [0, 0.5], plus 0.1 +- 0.02 sediment) with random wind angles, each eroded
+    for `cycles` cycles of `particles` particles by swe_batch_erode (mode
+    PARALLEL, the default) or swe_batch_erode_ordered (ORDERED). Returns (h0
+    [count,size,size], wind_xz [count,2], dh [count,size,size]) as float32
+    numpy arrays."""
+    rs = np.random.RandomState(seed)
+    h0 = np.empty((count, size, size), np.float32)
+    dh = np.empty((count, size, size), np.float32)
+    wind = np.empty((count, 2), np.float32)
+    for first in range(0, count, chunk):
+        k = min(chunk, count - first)
+        worlds = []
+        for i in range(k):
+            ang = rs.uniform(0.0, 2.0 * np.pi)
+            pers = rs.uniform(0.4, 0.6)
+            wx, wy, wz = wind_direction(float(np.cos(ang)), 0.0, float(np.sin(ang)))
+            wind[first + i] = (wx, wz)
+            w = World(size, params=Params(pspeed=(wx, wy, wz)), seed=int(seed * 1000003 + first + i + 1))
+            w.terrain(seed=int(seed * 7919 + first + i + 1), octaves=8, base_freq=1.0 / 64.0, persistence=pers,
+                      sediment=0.1, sediment_jitter=0.02)
+            worlds.append(w)
+        for i, w in enumerate(worlds):
+            h0[first + i] = w.height
+        batch_erode(worlds, cycles, particles, mode=mode)
+        for i, w in enumerate(worlds):
+            w.sync()
+            dh[first + i] = w.height - h0[first + i]
+            w.close()
+    return h0, wind, dh
+
+
+def rmse(a, b) -> float:
+    return float(np.sqrt(np.mean((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2)))
+
+
+class Rollout:
+    """Advances one terrain by jumps of `cycles` erode cycles: predicted by
+    the surrogate, with the plain method (PARALLEL, `particles` per cycle)
+    run over every `judge_every`-th jump as correction and judge. A jump whose
+    prediction misses the plain result by more than `bound` (height RMSE
+    relative to the plain result's height range) rejects the surrogate: it
+    and every later jump use the plain method."""
+
+    def __init__(self, model: Surrogate, size, wind, cycles=50, particles=1000, seed=1, judge_every=4, bound=0.01):
+        self.model, self.size, self.cycles, self.particles = model, size, cycles, particles
+        self.wind = wind_direction(*wind)
+        self.judge_every, self.bound = judge_every, bound
+        self.world = World(size, params=Params(pspeed=self.wind), seed=seed)
+        self.rejected = False
+        self.jumps = 0
+        self.judged = []  # relative RMSE of each judged jump
+
+    def start(self, height):
+        self.world.upload(Field.HEIGHT, np.asarray(height, np.float32))
+
+    def step(self):
+        torch = self.model.torch
+        h = self.world.height
+        self.jumps += 1
+        judge = self.rejected or self.jumps % self.judge_every == 0
+        pred = None
+        if not self.rejected:
+            hd = torch.from_numpy(h[None]).to(self.model.device)
+            wd = torch.tensor([[self.wind[0], self.wind[2]]], dtype=torch.float32, device=self.model.device)
+            pred = h + self.model.predict(hd, wd)[0].cpu().numpy()
+        if judge:
+            self.world.erode(self.particles, self.cycles, mode=Mode.PARALLEL)
+            plain = self.world.height
+            if pred is not None:
+                rel = rmse(pred, plain) / max(float(plain.max() - plain.min()), 1e-12)
+                self.judged.append(rel)
+                if rel > self.bound:
+                    self.rejected = True
+            return plain
+        self.world.upload(Field.HEIGHT, pred.astype(np.float32))
+        return pred
+
+    def close(self):
+        self.world.close()
