@@ -61,11 +61,15 @@ def parse_args():
     ap.add_argument("--lanes", type=int, default=0,
                     help="particles in flight: 0 = default (cells/64, min 1024), -1 = all at once")
     ap.add_argument("--no-all-at-once", action="store_true")
-    ap.add_argument("--workload", choices=["plain1024", "ensemble", "exact-ensemble"], default="plain1024",
+    ap.add_argument("--workload", choices=["plain1024", "ensemble", "exact-ensemble", "surrogate"],
+                    default="plain1024",
                     help="plain1024: the headline; ensemble: 64 terrains in one persistent launch; "
-                         "exact-ensemble: independent 256^2 worlds in ORDERED mode, one thread each")
+                         "exact-ensemble: independent 256^2 worlds in ORDERED mode, one thread each; "
+                         "surrogate: train the learned surrogate at 256^2 and measure it against the plain method")
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
     ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
+    ap.add_argument("--pairs", type=int, default=1024, help="surrogate: training pairs")
+    ap.add_argument("--train-steps", type=int, default=300, help="surrogate: timed Adam steps (batch 64)")
     ap.add_argument("--exact-size", type=int, default=256, help="exact-ensemble: map side")
     ap.add_argument("--cpu-sample", type=int, default=196608, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
@@ -690,6 +694,146 @@ def run_exact_ensemble(args):
         w.close()
 
 
+def run_surrogate(args):
+    """The learned surrogate at 256^2: training pairs of 50 cycles x 1000
+    particles made by the plain GPU method (PARALLEL, seeded fBm terrains of
+    persistence U[0.4, 0.6], random wind angles), `--train-steps` timed Adam
+    steps of batch 64 (lr 1e-3) after `--warmup` untimed ones, then on 64
+    held-out pairs: the network's RMSE of the change, the no-change RMSE and
+    the noise floor (the same held-out terrains eroded with other random
+    numbers); the time of one 50-cycle jump by the network and by the plain
+    method; and a judged rollout (8 jumps, the plain method every 4th). The
+    metric is the jump speed-up; the line carries the accuracy beside it."""
+    import torch
+
+    import simplewinderosion_gb300 as swe
+    from simplewinderosion_gb300 import surrogate as S
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    size, cycles, particles, batch = 256, 50, 1000, 64
+    t0 = time.perf_counter()
+    h_tr, w_tr, d_tr = S.make_pairs(args.pairs, size, cycles, particles, seed=21)
+    h_te, w_te, d_te = S.make_pairs(64, size, cycles, particles, seed=22)
+    _, _, d_te2 = S.make_pairs(64, size, cycles, particles, seed=22, erosion_seed=1)
+    gen_s = time.perf_counter() - t0
+
+    model = S.Surrogate(seed=1, scale=1.0 / max(float(d_tr.std()), 1e-9))
+    hd, wd, td = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (h_tr, w_tr, d_tr))
+    rs = np.random.RandomState(3)
+
+    def step():
+        idx = torch.from_numpy(rs.randint(0, args.pairs, batch)).to(dev)
+        return model.train_step(hd[idx].contiguous(), wd[idx].contiguous(), td[idx].contiguous(), lr=1e-3)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    losses = []
+    e0.record(stream)
+    for _ in range(args.train_steps):
+        losses.append(step())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1) / args.train_steps
+    flops = S.conv_flops(batch, size, size, backward=True)
+    tflops = flops / (train_ms / 1e3) / 1e12
+
+    # accuracy on held-out pairs
+    ht, wt = torch.from_numpy(h_te).to(dev), torch.from_numpy(w_te).to(dev)
+    pred = model.predict(ht, wt).cpu().numpy()
+    rng = float(np.mean([(h + d).max() - (h + d).min() for h, d in zip(h_te, d_te)]))
+    err_net, err_none, err_floor = S.rmse(pred, d_te), S.rmse(0 * d_te, d_te), S.rmse(d_te2, d_te)
+
+    # one 50-cycle jump of one terrain: network vs plain method
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        return best
+
+    one_h, one_w = ht[:1].contiguous(), wt[:1].contiguous()
+    sur_ms = timed(lambda: model.predict(one_h, one_w))
+    sur_batch_ms = timed(lambda: model.predict(ht, wt)) / 64
+    wind = (float(w_te[0, 0]), 0.0, float(w_te[0, 1]))
+    world = swe.World(size, params=swe.Params(pspeed=wind), seed=5)
+    world.upload(swe.Field.HEIGHT, h_te[0])
+    wstream = torch.cuda.ExternalStream(world.stream(), device=dev)
+    world.erode(particles, cycles, mode=swe.Mode.PARALLEL)
+    world.sync()
+    plain_ms = float("inf")
+    for _ in range(3):
+        world.upload(swe.Field.HEIGHT, h_te[0])
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(wstream)
+        world.erode(particles, cycles, mode=swe.Mode.PARALLEL, sync=False)
+        b.record(wstream)
+        world.sync()
+        plain_ms = min(plain_ms, a.elapsed_time(b))
+    world.close()
+
+    # judged rollout: 8 jumps, the plain method over every 4th
+    ro = S.Rollout(model, size, wind, cycles=cycles, particles=particles, seed=9, judge_every=4, bound=0.01)
+    ro.start(h_te[0])
+    t1 = time.perf_counter()
+    for _ in range(8):
+        ro.step()
+    roll_s = time.perf_counter() - t1
+    judged, rejected = ro.judged, ro.rejected
+    ro.close()
+
+    peak, peak_note = 1900.0, "fallback"
+    try:
+        peak = float(json.loads(PEAKS_FILE.read_text())["bf16_tflops_sustained"])
+        peak_note = "measured (sustained)"
+    except Exception:
+        pass
+    line = {
+        "metric": "surrogate speed-up over plain GPU erosion, one 50-cycle jump of a 256^2 terrain",
+        "value": plain_ms / sur_ms,
+        "unit": "x",
+        "n_gpus": 1,
+        "steps": args.train_steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": train_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16 (fp32 accumulate)",
+        "data": "synthetic",
+        "config": {"workload": f"U-Net 32/64/96/128 at 256^2, {args.pairs} training pairs of 50 cycles x 1000 "
+                               f"particles (PARALLEL plain method), batch 64, Adam lr 1e-3, "
+                               f"{args.train_steps} timed steps",
+                   "pairs": args.pairs, "pair_generation_s": gen_s, "l2": "activations of a batch exceed L2"},
+        "surrogate": {"jump_ms": sur_ms, "jump_ms_per_terrain_batch64": sur_batch_ms, "plain_jump_ms": plain_ms,
+                      "speedup_batch64": plain_ms / sur_batch_ms,
+                      "heldout_rmse_change": {"network": err_net, "no_change": err_none, "noise_floor": err_floor},
+                      "heldout_rel_rmse": {"network": err_net / rng, "no_change": err_none / rng,
+                                           "noise_floor": err_floor / rng},
+                      "gain_over_no_change": 1.0 - err_net / err_none,
+                      "loss_first_last": [float(np.mean(losses[:10])), float(np.mean(losses[-10:]))],
+                      "rollout": {"jumps": 8, "judge_every": 4, "judged_rel_rmse": judged, "rejected": rejected,
+                                  "seconds": roll_s}},
+        "roofline": {"bound": "tensor", "kernel": "k_conv3x3 + k_conv_wgrad (warp-level mma.sync m16n8k16)",
+                     "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                     "peak_source": peak_note, "flops_per_step": flops, "traffic": None},
+        "gpu_launches": 126 * args.train_steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -698,6 +842,8 @@ def main():
         run_ensemble(args)
     elif args.workload == "exact-ensemble":
         run_exact_ensemble(args)
+    elif args.workload == "surrogate":
+        run_surrogate(args)
     else:
         run_ours(args)
 

@@ -280,14 +280,33 @@ class Surrogate:
         return ch0
 
 
-def make_pairs(count, size=256, cycles=50, particles=1000, seed=0, chunk=2048, mode=Mode.PARALLEL):
+# map-side divisor of each layer's resolution
+_LEVEL = {"in": 1, "e0": 1, "d1": 2, "d2": 4, "d3": 8, "b3": 8, "u2": 4, "u1": 2, "u0": 1, "out": 1}
+
+
+def conv_flops(n, h, w, backward=False) -> float:
+    """Multiply-add FLOPs (2 per MAC, padded channels included) of the
+    network's convolutions for n maps of h x w: the forward pass, or the
+    forward pass plus the input and weight gradients of a training step."""
+    total = 0.0
+    for name, cin, cout in LAYERS:
+        f = 2.0 * cin * cout * 9 * n * (h // _LEVEL[name]) * (w // _LEVEL[name])
+        total += f
+        if backward:
+            total += f * (1 if name == "in" else 2)
+    return total
+
+
+def make_pairs(count, size=256, cycles=50, particles=1000, seed=0, chunk=2048, mode=Mode.PARALLEL,
+               erosion_seed=0):
     """Training pairs from the erosion path: `count` seeded fBm terrains
     (8 octaves, base frequency 1/64, persistence uniform in [0.4, 0.6], in
     [0, 0.5], plus 0.1 +- 0.02 sediment) with random wind angles, each eroded
     for `cycles` cycles of `particles` particles by swe_batch_erode (mode
-    PARALLEL, the default) or swe_batch_erode_ordered (ORDERED). Returns (h0
-    [count,size,size], wind_xz [count,2], dh [count,size,size]) as float32
-    numpy arrays."""
+    PARALLEL, the default) or swe_batch_erode_ordered (ORDERED);
+    `erosion_seed` changes the erosion's random numbers and not the
+    terrains. Returns (h0 [count,size,size], wind_xz [count,2], dh
+    [count,size,size]) as float32 numpy arrays."""
     rs = np.random.RandomState(seed)
     h0 = np.empty((count, size, size), np.float32)
     dh = np.empty((count, size, size), np.float32)
@@ -300,7 +319,8 @@ def make_pairs(count, size=256, cycles=50, particles=1000, seed=0, chunk=2048, m
             pers = rs.uniform(0.4, 0.6)
             wx, wy, wz = wind_direction(float(np.cos(ang)), 0.0, float(np.sin(ang)))
             wind[first + i] = (wx, wz)
-            w = World(size, params=Params(pspeed=(wx, wy, wz)), seed=int(seed * 1000003 + first + i + 1))
+            w = World(size, params=Params(pspeed=(wx, wy, wz)),
+                      seed=int(seed * 1000003 + first + i + 1 + erosion_seed * 7777777))
             w.terrain(seed=int(seed * 7919 + first + i + 1), octaves=8, base_freq=1.0 / 64.0, persistence=pers,
                       sediment=0.1, sediment_jitter=0.02)
             worlds.append(w)
