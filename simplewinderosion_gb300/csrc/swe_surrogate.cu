@@ -5,10 +5,12 @@
 //   k_conv3x3       y = conv3x3(x, w) + b as an implicit GEMM on the tensor
 //                   cores (warp-level mma m16n8k16, bf16 in, fp32 out):
 //                   rows = pixels, columns = output channels, K = 9 taps x
-//                   input channels. The input gradient is the same kernel on
+//                   input channels, tiles staged in shared memory and read
+//                   by ldmatrix. The input gradient is the same kernel on
 //                   dy with the weights flipped and transposed (k_flip).
-//   k_conv_wgrad    dW += dy^T x_shifted, an implicit GEMM with K = pixels,
-//                   split over pixel chunks and reduced with fp32 atomics.
+//   k_conv_wgrad    dW += dy^T x_shifted, an implicit GEMM with K = pixels:
+//                   pixel tiles staged in shared memory, fragments by
+//                   ldmatrix .trans, pixel chunks reduced with fp32 atomics.
 //   k_bias_grad     db += sum over pixels of dy.
 //   elementwise     GELU (erf form) and its derivative, 2x2 average pooling,
 //                   nearest 2x upsampling and their adjoints, adds, the
@@ -25,8 +27,6 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
 __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
   return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
@@ -42,33 +42,45 @@ __device__ __forceinline__ void mma16816(float (&c)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-constexpr int kConvNT = 4;  // output-channel tiles of 8 per warp
+constexpr int kConvNT = 4;     // output-channel tiles of 8 per warp (32 channels)
+constexpr int kConvPix = 64;   // pixels per block (4 warps x 16)
+constexpr int kConvK = 32;     // input channels per stage
+constexpr int kConvStride = 40;  // smem row stride in bf16 (80 bytes)
 
-// One warp: 16 pixels x 32 output channels. Lane (g = lane/4, t = lane%4)
-// holds rows g and g+8 of the pixel tile and columns 2t, 2t+1 of each
-// 8-channel tile. Requires cin % 16 == 0 and cout % 8 == 0.
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const bf16* p) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(a));
+}
+
+// One block: 64 pixels x 32 output channels, 4 warps of 16 pixels x 32
+// channels. For every tap and 32-channel slice of the input, the block
+// copies the tap-shifted input rows (64 pixels x 32 channels, zero outside
+// the map) and the weights (32 output x 32 input channels) into shared
+// memory with 16-byte loads; ldmatrix hands out the fragments (A: pixels x
+// input channels, B: input x output channels). Requires cin % 8 == 0 and
+// cout % 8 == 0.
 __global__ void __launch_bounds__(128) k_conv3x3(const bf16* __restrict__ x, const bf16* __restrict__ w,
                                                  const float* __restrict__ bias, bf16* __restrict__ y, int N, int H,
                                                  int W, int cin, int cout) {
+  __shared__ __align__(16) bf16 sa[kConvPix * kConvStride];
+  __shared__ __align__(16) bf16 sb[8 * kConvNT * kConvStride];
   const long M = (long)N * H * W;
-  const long mtiles = (M + 15) / 16;
-  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  const int cblocks = (cout + 8 * kConvNT - 1) / (8 * kConvNT);
-  if (warp >= mtiles * cblocks) return;
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const long m0 = (warp % mtiles) * 16;
-  const int co0 = (int)(warp / mtiles) * 8 * kConvNT;
-
-  long pr[2];
-  int py[2], px[2];
-  bool in[2];
+  const long m0 = (long)blockIdx.x * kConvPix;
+  const int co0 = blockIdx.y * 8 * kConvNT;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3, mi = lane >> 3, r = lane & 7;
+  // staging of A: thread -> pixel rows tid/4 and 32 + tid/4, 8-channel segment
+  const int arow = tid >> 2, aseg = (tid & 3) * 8;
+  long ap[2];
+  int apx[2], apy[2];
 #pragma unroll
-  for (int r = 0; r < 2; r++) {
-    pr[r] = m0 + g + 8 * r;
-    in[r] = pr[r] < M;
-    const long p = in[r] ? pr[r] : 0;
-    px[r] = (int)(p % W);
-    py[r] = (int)((p / W) % H);
+  for (int h = 0; h < 2; h++) {
+    ap[h] = m0 + arow + 32 * h;
+    const long pp = ap[h] < M ? ap[h] : 0;
+    apx[h] = (int)(pp % W);
+    apy[h] = (int)((pp / W) % H);
   }
   float acc[kConvNT][4];
 #pragma unroll
@@ -78,28 +90,35 @@ __global__ void __launch_bounds__(128) k_conv3x3(const bf16* __restrict__ x, con
 
   for (int tap = 0; tap < 9; tap++) {
     const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const bf16* src[2];
+    for (int c0 = 0; c0 < cin; c0 += kConvK) {
+      uint4 va[2], vb = make_uint4(0, 0, 0, 0);
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      const int yy = py[r] + dy, xx = px[r] + dx;
-      const bool ok = in[r] && yy >= 0 && yy < H && xx >= 0 && xx < W;
-      src[r] = ok ? x + (pr[r] + (long)dy * W + dx) * cin : nullptr;
-    }
-    for (int ci0 = 0; ci0 < cin; ci0 += 16) {
-      const uint32_t a0 = src[0] ? ld_pair(src[0] + ci0 + 2 * t) : 0u;
-      const uint32_t a1 = src[1] ? ld_pair(src[1] + ci0 + 2 * t) : 0u;
-      const uint32_t a2 = src[0] ? ld_pair(src[0] + ci0 + 2 * t + 8) : 0u;
-      const uint32_t a3 = src[1] ? ld_pair(src[1] + ci0 + 2 * t + 8) : 0u;
+      for (int h = 0; h < 2; h++) {
+        va[h] = make_uint4(0, 0, 0, 0);
+        const int yy = apy[h] + dy, xx = apx[h] + dx;
+        if (ap[h] < M && c0 + aseg < cin && yy >= 0 && yy < H && xx >= 0 && xx < W)
+          va[h] = *reinterpret_cast<const uint4*>(x + (ap[h] + (long)dy * W + dx) * cin + c0 + aseg);
+      }
+      if (co0 + arow < cout && c0 + aseg < cin)
+        vb = *reinterpret_cast<const uint4*>(w + ((long)(co0 + arow) * 9 + tap) * cin + c0 + aseg);
+      __syncthreads();  // the previous stage's fragments are read
 #pragma unroll
-      for (int j = 0; j < kConvNT; j++) {
-        const int co = co0 + 8 * j + g;
-        uint32_t b0 = 0u, b1 = 0u;
-        if (co < cout) {
-          const bf16* wp = w + ((long)co * 9 + tap) * cin + ci0 + 2 * t;
-          b0 = ld_pair(wp);
-          b1 = ld_pair(wp + 8);
+      for (int h = 0; h < 2; h++) *reinterpret_cast<uint4*>(sa + (arow + 32 * h) * kConvStride + aseg) = va[h];
+      *reinterpret_cast<uint4*>(sb + arow * kConvStride + aseg) = vb;
+      __syncthreads();
+#pragma unroll
+      for (int k0 = 0; k0 < kConvK; k0 += 16) {
+        uint32_t a0, a1, a2, a3;
+        // A (16 px x 16 ci): matrices (px 0-7 | 8-15) x (ci 0-7 | 8-15)
+        ldsm_x4(a0, a1, a2, a3, sa + (warp * 16 + r + ((mi & 1) << 3)) * kConvStride + k0 + ((mi >> 1) << 3));
+#pragma unroll
+        for (int j = 0; j < kConvNT; j += 2) {
+          // B for output-channel tiles j, j+1: (co 0-7 | 8-15) x (ci 0-7 | 8-15)
+          uint32_t b0, b1, b2, b3;
+          ldsm_x4(b0, b1, b2, b3, sb + (8 * j + r + ((mi >> 1) << 3)) * kConvStride + k0 + ((mi & 1) << 3));
+          mma16816(acc[j], a0, a1, a2, a3, b0, b1);
+          mma16816(acc[j + 1], a0, a1, a2, a3, b2, b3);
         }
-        mma16816(acc[j], a0, a1, a2, a3, b0, b1);
       }
     }
   }
@@ -109,10 +128,11 @@ __global__ void __launch_bounds__(128) k_conv3x3(const bf16* __restrict__ x, con
     if (co >= cout) continue;
     const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      if (!in[r]) continue;
-      const uint32_t v = pack2(__float2bfloat16_rn(acc[j][2 * r] + b0), __float2bfloat16_rn(acc[j][2 * r + 1] + b1));
-      *reinterpret_cast<uint32_t*>(y + pr[r] * cout + co) = v;
+    for (int r2 = 0; r2 < 2; r2++) {
+      const long p = m0 + warp * 16 + g + 8 * r2;
+      if (p >= M) continue;
+      const uint32_t v = pack2(__float2bfloat16_rn(acc[j][2 * r2] + b0), __float2bfloat16_rn(acc[j][2 * r2 + 1] + b1));
+      *reinterpret_cast<uint32_t*>(y + p * cout + co) = v;
     }
   }
 }
@@ -130,81 +150,90 @@ __global__ void k_flip(const bf16* __restrict__ w, bf16* __restrict__ wf, int ci
   }
 }
 
-constexpr int kWgNT = 2;        // 8-column tiles (tap, input channel) per warp
-constexpr int kWgChunk = 256;   // pixels per warp (16 mma k-steps)
+// Weight gradient tiles: one block = 32 output x 32 input channels of one
+// tap over a chunk of pixels; 4 warps, each 16 x 16 (two 8-column mma
+// tiles); pixels staged 32 at a time (two mma k-steps).
+constexpr int kWgTile = 32;
+constexpr int kWgPix = 32;
+constexpr int kWgChunk = 4096;  // pixels per block
+constexpr int kWgStride = 40;   // smem row stride in bf16 (80 bytes: 16-byte aligned rows, fewer conflicts)
 
-__device__ __forceinline__ bf16 ld_bf16(const bf16* p) { return *p; }
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3,
+                                              const bf16* p) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(a));
+}
 
-// dW[co][tap][ci] += sum_p dy[p][co] x[p + off(tap)][ci]: rows = output
-// channels (16 per warp), columns = (tap, ci) (8 kWgNT per warp, within one
-// tap since cin % 16 == 0), K = a chunk of kWgChunk pixels.
+// dW[co][tap][ci] += sum_p dy[p][co] x[p + off(tap)][ci] (zero padding).
+// As a GEMM: rows co, columns ci, K = pixels. Each stage copies 32 pixels
+// of dy (32 channels from co0) and of the tap-shifted x (32 channels from
+// ci0) into shared memory, rows = pixels, with 16-byte loads; ldmatrix
+// .trans then hands out the fragments (A = dy^T, B = x, both with pixel
+// pairs per register). Channels past cout / cin and pixels past the map or
+// the batch are zero. The block's 32 x 32 partial sums go to dw with fp32
+// atomics. Requires cin % 8 == 0 and cout % 8 == 0.
 __global__ void __launch_bounds__(128) k_conv_wgrad(const bf16* __restrict__ x, const bf16* __restrict__ dy,
                                                     float* __restrict__ dw, int N, int H, int W, int cin, int cout) {
+  __shared__ __align__(16) bf16 sdy[kWgPix * kWgStride];
+  __shared__ __align__(16) bf16 sx[kWgPix * kWgStride];
   const long M = (long)N * H * W;
-  const long chunks = (M + kWgChunk - 1) / kWgChunk;
-  const int rtiles = (cout + 15) / 16;
-  const int ctiles = (9 * cin) / (8 * kWgNT);
-  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  if (warp >= chunks * rtiles * ctiles) return;
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const long chunk = warp % chunks;
-  const int rt = (int)((warp / chunks) % rtiles);
-  const int ct = (int)(warp / (chunks * rtiles));
-  const int co_a = rt * 16 + g, co_b = co_a + 8;
-  float acc[kWgNT][4];
+  const int ctile = (cin + kWgTile - 1) / kWgTile;
+  int by = blockIdx.y;
+  const int tap = by % 9;
+  by /= 9;
+  const int ci0 = (by % ctile) * kWgTile;
+  const int co0 = (by / ctile) * kWgTile;
+  const int ddy = tap / 3 - 1, ddx = tap % 3 - 1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp >> 1) * 16, wn = (warp & 1) * 16;  // the warp's co / ci offsets in the tile
+  // staging: thread -> (pixel row, 8-channel segment)
+  const int srow = tid >> 2, sseg = (tid & 3) * 8;
+  float acc[2][4];
 #pragma unroll
-  for (int j = 0; j < kWgNT; j++)
+  for (int j = 0; j < 2; j++)
 #pragma unroll
     for (int q = 0; q < 4; q++) acc[j][q] = 0.0f;
-  const bf16 zero = __float2bfloat16_rn(0.0f);
 
-  for (int k0 = 0; k0 < kWgChunk; k0 += 16) {
-    // the four pixels of this lane in the k-step: 2t, 2t+1, 2t+8, 2t+9
-    long p[4];
-    bool pin[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      p[q] = chunk * kWgChunk + k0 + 2 * t + (q & 1) + 8 * (q >> 1);
-      pin[q] = p[q] < M;
+  const long pbeg = (long)blockIdx.x * kWgChunk;
+  const long pend = pbeg + kWgChunk < M ? pbeg + kWgChunk : M;
+  for (long p0 = pbeg; p0 < pend; p0 += kWgPix) {
+    const long p = p0 + srow;
+    uint4 vdy = make_uint4(0, 0, 0, 0), vx = make_uint4(0, 0, 0, 0);
+    if (p < pend) {
+      if (co0 + sseg < cout) vdy = *reinterpret_cast<const uint4*>(dy + p * cout + co0 + sseg);
+      const int xx = (int)(p % W) + ddx, yy = (int)((p / W) % H) + ddy;
+      if (ci0 + sseg < cin && xx >= 0 && xx < W && yy >= 0 && yy < H)
+        vx = *reinterpret_cast<const uint4*>(x + (p + (long)ddy * W + ddx) * cin + ci0 + sseg);
     }
-    bf16 va[4], vb[4];
+    __syncthreads();  // the previous stage's fragments are read
+    *reinterpret_cast<uint4*>(sdy + srow * kWgStride + sseg) = vdy;
+    *reinterpret_cast<uint4*>(sx + srow * kWgStride + sseg) = vx;
+    __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      va[q] = (pin[q] && co_a < cout) ? ld_bf16(dy + p[q] * cout + co_a) : zero;
-      vb[q] = (pin[q] && co_b < cout) ? ld_bf16(dy + p[q] * cout + co_b) : zero;
-    }
-    const uint32_t a0 = pack2(va[0], va[1]), a1 = pack2(vb[0], vb[1]);
-    const uint32_t a2 = pack2(va[2], va[3]), a3 = pack2(vb[2], vb[3]);
-#pragma unroll
-    for (int j = 0; j < kWgNT; j++) {
-      const int col = (ct * kWgNT + j) * 8 + g;  // (tap, ci) column of this lane
-      const int tap = col / cin, ci = col % cin;
-      const int ddy = tap / 3 - 1, ddx = tap % 3 - 1;
-      bf16 vx[4];
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        bool ok = pin[q];
-        long src = 0;
-        if (ok) {
-          const int xx = (int)(p[q] % W) + ddx, yy = (int)((p[q] / W) % H) + ddy;
-          ok = xx >= 0 && xx < W && yy >= 0 && yy < H;
-          src = p[q] + (long)ddy * W + ddx;
-        }
-        vx[q] = ok ? ld_bf16(x + src * cin + ci) : zero;
-      }
-      mma16816(acc[j], a0, a1, a2, a3, pack2(vx[0], vx[1]), pack2(vx[2], vx[3]));
+    for (int k0 = 0; k0 < kWgPix; k0 += 16) {
+      // A (16 co x 16 px): matrices (co 0-7 | 8-15) x (px 0-7 | 8-15)
+      const int mi = lane >> 3, r = lane & 7;
+      uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
+      ldsm_x4_trans(a0, a1, a2, a3, sdy + (k0 + r + ((mi >> 1) << 3)) * kWgStride + wm + ((mi & 1) << 3));
+      // B (16 px x 16 ci): matrices (px 0-7 | 8-15) x (ci 0-7 | 8-15)
+      ldsm_x4_trans(b0, b1, b2, b3, sx + (k0 + r + ((mi & 1) << 3)) * kWgStride + wn + ((mi >> 1) << 3));
+      mma16816(acc[0], a0, a1, a2, a3, b0, b1);
+      mma16816(acc[1], a0, a1, a2, a3, b2, b3);
     }
   }
+  const int g = lane >> 2, t = lane & 3;
 #pragma unroll
-  for (int j = 0; j < kWgNT; j++) {
-    const int col = (ct * kWgNT + j) * 8 + 2 * t;
+  for (int j = 0; j < 2; j++) {
+    const int ci = ci0 + wn + 8 * j + 2 * t;
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      const int co = r ? co_b : co_a;
-      if (co >= cout) continue;
-      // dw layout [co][tap][ci] = [co][col]
-      atomicAdd(dw + (long)co * 9 * cin + col, acc[j][2 * r]);
-      atomicAdd(dw + (long)co * 9 * cin + col + 1, acc[j][2 * r + 1]);
+    for (int r2 = 0; r2 < 2; r2++) {
+      const int co = co0 + wm + g + 8 * r2;
+      if (co >= cout || ci >= cin) continue;
+      float* o = dw + ((long)co * 9 + tap) * cin + ci;
+      atomicAdd(o, acc[j][2 * r2]);
+      atomicAdd(o + 1, acc[j][2 * r2 + 1]);
     }
   }
 }
@@ -369,10 +398,11 @@ inline unsigned grid_for(long n, int threads = 256) {
 cudaError_t nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int N, int H, int W, int cin,
                        int cout, cudaStream_t s) {
   const long M = (long)N * H * W;
-  const long warps = ((M + 15) / 16) * ((cout + 8 * kConvNT - 1) / (8 * kConvNT));
-  const long blocks = (warps * 32 + 127) / 128;
-  k_conv3x3<<<(unsigned)blocks, 128, 0, s>>>(static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias,
-                                             static_cast<bf16*>(y), N, H, W, cin, cout);
+  const long blocks = (M + kConvPix - 1) / kConvPix;
+  const int cblocks = (cout + 8 * kConvNT - 1) / (8 * kConvNT);
+  if (blocks > 0x7fffffffL || cblocks > 65535) return cudaErrorInvalidValue;
+  k_conv3x3<<<dim3((unsigned)blocks, (unsigned)cblocks), 128, 0, s>>>(
+      static_cast<const bf16*>(x), static_cast<const bf16*>(w), bias, static_cast<bf16*>(y), N, H, W, cin, cout);
   return cudaGetLastError();
 }
 
@@ -385,10 +415,12 @@ cudaError_t nn_flip(const void* w, void* wf, int cin, int cout, cudaStream_t s) 
 cudaError_t nn_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int N, int H, int W, int cin, int cout,
                           cudaStream_t s) {
   const long M = (long)N * H * W;
-  const long warps = ((M + kWgChunk - 1) / kWgChunk) * ((cout + 15) / 16) * ((9 * cin) / (8 * kWgNT));
-  const long blocks = (warps * 32 + 127) / 128;
-  k_conv_wgrad<<<(unsigned)blocks, 128, 0, s>>>(static_cast<const bf16*>(x), static_cast<const bf16*>(dy), dw, N, H,
-                                                W, cin, cout);
+  const long chunks = (M + kWgChunk - 1) / kWgChunk;
+  const int tiles = 9 * ((cin + kWgTile - 1) / kWgTile) * ((cout + kWgTile - 1) / kWgTile);
+  if (chunks > 0x7fffffffL || tiles > 65535) return cudaErrorInvalidValue;
+  k_conv_wgrad<<<dim3((unsigned)chunks, (unsigned)tiles), 128, 0, s>>>(static_cast<const bf16*>(x),
+                                                                      static_cast<const bf16*>(dy), dw, N, H, W, cin,
+                                                                      cout);
   if (db) {
     long bx = (M + 255) / 256;
     if (bx > 64) bx = 64;
