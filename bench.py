@@ -69,7 +69,7 @@ def parse_args():
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
     ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
     ap.add_argument("--pairs", type=int, default=1024, help="surrogate: training pairs")
-    ap.add_argument("--train-steps", type=int, default=300, help="surrogate: timed Adam steps (batch 64)")
+    ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed Adam steps (batch 64)")
     ap.add_argument("--exact-size", type=int, default=256, help="exact-ensemble: map side")
     ap.add_argument("--cpu-sample", type=int, default=196608, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
