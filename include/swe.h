@@ -334,10 +334,13 @@ int swe_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int
 int swe_nn_conv3x3_flip(const void* w, void* wf, int cin, int cout, void* stream);
 /* Weight and bias gradients of swe_nn_conv3x3, ADDED to dw (fp32
  * [cout,3,3,cin]) and db (fp32 [cout], or NULL) from its input x and the
- * output gradient dy (bf16 [n,h,w,cout]). */
+ * output gradient dy (bf16 [n,h,w,cout]); cout <= 256, x and dy 16-byte
+ * aligned. */
 int swe_nn_conv3x3_wgrad(const void* x, const void* dy, float* dw, float* db, int n, int h, int wd, int cin, int cout,
                          void* stream);
-/* act = GELU(pre) = pre (1 + erf(pre / sqrt 2)) / 2, and dpre = dact GELU'(pre). */
+/* act = GELU(pre) = pre (1 + erf(pre / sqrt 2)) / 2, and dpre = dact GELU'(pre).
+ * For these and the pooling, upsampling and add calls: counts and channel
+ * numbers are multiples of 8 and tensors 16-byte aligned. */
 int swe_nn_gelu(const void* pre, void* act, int64_t count, void* stream);
 int swe_nn_gelu_bwd(const void* pre, const void* dact, void* dpre, int64_t count, void* stream);
 /* 2x2 average pooling of x [n,h,w,c] (h, w even) into y [n,h/2,w/2,c]; with

@@ -238,15 +238,29 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const bf16* __restrict__ x, 
   }
 }
 
-// db[co] += sum_p dy[p][co]: each thread sums a strided run of pixels of one
-// channel, one atomic per thread.
+// db[co] += sum_p dy[p][co]. Thread -> (pixel row, 8-channel group) with
+// 16-byte loads; per-thread sums go to shared-memory accumulators, then one
+// global atomic per channel per block. cout % 8 == 0, cout <= 256.
 __global__ void k_bias_grad(const bf16* __restrict__ dy, float* __restrict__ db, long M, int cout) {
-  const int co = blockIdx.y;
-  float s = 0.0f;
-  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < M; p += (long)gridDim.x * blockDim.x)
-    s += __bfloat162float(dy[p * cout + co]);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(db + co, s);
+  __shared__ float sdb[256];
+  const int groups = cout / 8;
+  const int rows = blockDim.x / groups;
+  for (int c = threadIdx.x; c < cout; c += blockDim.x) sdb[c] = 0.0f;
+  __syncthreads();
+  if ((int)threadIdx.x < rows * groups) {
+    const int grp = threadIdx.x % groups, row = threadIdx.x / groups;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long p = (long)blockIdx.x * rows + row; p < M; p += (long)gridDim.x * rows) {
+      const uint4 v = *reinterpret_cast<const uint4*>(dy + p * cout + grp * 8);
+      const bf16* e = reinterpret_cast<const bf16*>(&v);
+#pragma unroll
+      for (int k = 0; k < 8; k++) acc[k] += __bfloat162float(e[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) atomicAdd(&sdb[grp * 8 + k], acc[k]);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < cout; c += blockDim.x) atomicAdd(db + c, sdb[c]);
 }
 
 __device__ __forceinline__ float gelu(float v) { return 0.5f * v * (1.0f + erff(v * 0.70710678f)); }
@@ -254,77 +268,137 @@ __device__ __forceinline__ float gelu_grad(float v) {
   return 0.5f * (1.0f + erff(v * 0.70710678f)) + v * 0.39894228f * expf(-0.5f * v * v);
 }
 
-__global__ void k_gelu(const bf16* __restrict__ pre, bf16* __restrict__ act, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    act[i] = __float2bfloat16_rn(gelu(__bfloat162float(pre[i])));
+// The elementwise kernels move 8 bf16 values (16 bytes) per thread step;
+// counts and channel numbers are multiples of 8 (checked by the callers).
+struct Vec8 {
+  float v[8];
+  __device__ __forceinline__ void load(const bf16* p) {
+    const uint4 u = *reinterpret_cast<const uint4*>(p);
+    const bf16* e = reinterpret_cast<const bf16*>(&u);
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = __bfloat162float(e[k]);
+  }
+  __device__ __forceinline__ void store(bf16* p) const {
+    uint4 u;
+    bf16* e = reinterpret_cast<bf16*>(&u);
+#pragma unroll
+    for (int k = 0; k < 8; k++) e[k] = __float2bfloat16_rn(v[k]);
+    *reinterpret_cast<uint4*>(p) = u;
+  }
+};
+
+__global__ void k_gelu(const bf16* __restrict__ pre, bf16* __restrict__ act, long n8) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n8; i += (long)gridDim.x * blockDim.x) {
+    Vec8 a;
+    a.load(pre + 8 * i);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] = gelu(a.v[k]);
+    a.store(act + 8 * i);
+  }
 }
 
 __global__ void k_gelu_bwd(const bf16* __restrict__ pre, const bf16* __restrict__ dact, bf16* __restrict__ dpre,
-                           long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    dpre[i] = __float2bfloat16_rn(__bfloat162float(dact[i]) * gelu_grad(__bfloat162float(pre[i])));
+                           long n8) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n8; i += (long)gridDim.x * blockDim.x) {
+    Vec8 a, d;
+    a.load(pre + 8 * i);
+    d.load(dact + 8 * i);
+#pragma unroll
+    for (int k = 0; k < 8; k++) d.v[k] = d.v[k] * gelu_grad(a.v[k]);
+    d.store(dpre + 8 * i);
+  }
 }
 
 // y[n][i][j][c] = mean of x[n][2i..2i+1][2j..2j+1][c] (H, W even: the input's).
 __global__ void k_pool2(const bf16* __restrict__ x, bf16* __restrict__ y, int N, int H, int W, int C) {
-  const int Ho = H / 2, Wo = W / 2;
-  const long n = (long)N * Ho * Wo * C;
+  const int Ho = H / 2, Wo = W / 2, G = C / 8;
+  const long n = (long)N * Ho * Wo * G;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const long q = i / C;
+    const int c = (int)(i % G) * 8;
+    const long q = i / G;
     const int j = (int)(q % Wo), ii = (int)((q / Wo) % Ho);
     const long b = q / ((long)Wo * Ho);
     const long s = ((b * H + 2 * ii) * W + 2 * j) * C + c;
-    const float v = __bfloat162float(x[s]) + __bfloat162float(x[s + C]) + __bfloat162float(x[s + (long)W * C]) +
-                    __bfloat162float(x[s + (long)W * C + C]);
-    y[i] = __float2bfloat16_rn(0.25f * v);
+    Vec8 a, t;
+    a.load(x + s);
+    t.load(x + s + C);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
+    t.load(x + s + (long)W * C);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
+    t.load(x + s + (long)W * C + C);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] = 0.25f * (a.v[k] + t.v[k]);
+    a.store(y + q * C + c);
   }
 }
 
 // dx[n][y][x][c] = dy[n][y/2][x/2][c] / 4 (H, W: the pooling's input).
 __global__ void k_pool2_bwd(const bf16* __restrict__ dy, bf16* __restrict__ dx, int N, int H, int W, int C) {
-  const long n = (long)N * H * W * C;
+  const int G = C / 8;
+  const long n = (long)N * H * W * G;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const long q = i / C;
+    const int c = (int)(i % G) * 8;
+    const long q = i / G;
     const int xx = (int)(q % W), yy = (int)((q / W) % H);
     const long b = q / ((long)W * H);
-    dx[i] = __float2bfloat16_rn(0.25f * __bfloat162float(dy[((b * (H / 2) + yy / 2) * (W / 2) + xx / 2) * C + c]));
+    Vec8 a;
+    a.load(dy + ((b * (H / 2) + yy / 2) * (W / 2) + xx / 2) * C + c);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] *= 0.25f;
+    a.store(dx + q * C + c);
   }
 }
 
 // y[n][y][x][c] = x[n][y/2][x/2][c] (H, W: the input's; the output is 2H x 2W).
 __global__ void k_up2(const bf16* __restrict__ x, bf16* __restrict__ y, int N, int H, int W, int C) {
-  const int Ho = 2 * H, Wo = 2 * W;
-  const long n = (long)N * Ho * Wo * C;
+  const int Ho = 2 * H, Wo = 2 * W, G = C / 8;
+  const long n = (long)N * Ho * Wo * G;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const long q = i / C;
+    const int c = (int)(i % G) * 8;
+    const long q = i / G;
     const int xx = (int)(q % Wo), yy = (int)((q / Wo) % Ho);
     const long b = q / ((long)Wo * Ho);
-    y[i] = x[((b * H + yy / 2) * W + xx / 2) * C + c];
+    *reinterpret_cast<uint4*>(y + q * C + c) =
+        *reinterpret_cast<const uint4*>(x + ((b * H + yy / 2) * W + xx / 2) * C + c);
   }
 }
 
 // dx[n][i][j][c] = sum of dy over the 2x2 block (H, W: the upsampling's input).
 __global__ void k_up2_bwd(const bf16* __restrict__ dy, bf16* __restrict__ dx, int N, int H, int W, int C) {
-  const long n = (long)N * H * W * C;
-  const int Wo = 2 * W;
+  const int G = C / 8, Wo = 2 * W;
+  const long n = (long)N * H * W * G;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const long q = i / C;
+    const int c = (int)(i % G) * 8;
+    const long q = i / G;
     const int j = (int)(q % W), ii = (int)((q / W) % H);
     const long b = q / ((long)W * H);
     const long s = ((b * 2 * H + 2 * ii) * Wo + 2 * j) * C + c;
-    const float v = __bfloat162float(dy[s]) + __bfloat162float(dy[s + C]) + __bfloat162float(dy[s + (long)Wo * C]) +
-                    __bfloat162float(dy[s + (long)Wo * C + C]);
-    dx[i] = __float2bfloat16_rn(v);
+    Vec8 a, t;
+    a.load(dy + s);
+    t.load(dy + s + C);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
+    t.load(dy + s + (long)Wo * C);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
+    t.load(dy + s + (long)Wo * C + C);
+#pragma unroll
+    for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
+    a.store(dx + q * C + c);
   }
 }
 
-__global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf16* __restrict__ out, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    out[i] = __float2bfloat16_rn(__bfloat162float(a[i]) + __bfloat162float(b[i]));
+__global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf16* __restrict__ out, long n8) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n8; i += (long)gridDim.x * blockDim.x) {
+    Vec8 u, v;
+    u.load(a + 8 * i);
+    v.load(b + 8 * i);
+#pragma unroll
+    for (int k = 0; k < 8; k++) u.v[k] += v.v[k];
+    u.store(out + 8 * i);
+  }
 }
 
 // Network input, 16 channels per pixel: (height - 0.25) * 4, the wind
@@ -423,44 +497,44 @@ cudaError_t nn_conv_wgrad(const void* x, const void* dy, float* dw, float* db, i
                                                                       cout);
   if (db) {
     long bx = (M + 255) / 256;
-    if (bx > 64) bx = 64;
-    k_bias_grad<<<dim3((unsigned)bx, (unsigned)cout), 256, 0, s>>>(static_cast<const bf16*>(dy), db, M, cout);
+    if (bx > 1024) bx = 1024;
+    k_bias_grad<<<(unsigned)bx, 256, 0, s>>>(static_cast<const bf16*>(dy), db, M, cout);
   }
   return cudaGetLastError();
 }
 
 cudaError_t nn_gelu(const void* pre, void* act, long n, cudaStream_t s) {
-  k_gelu<<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(pre), static_cast<bf16*>(act), n);
+  k_gelu<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(pre), static_cast<bf16*>(act), n / 8);
   return cudaGetLastError();
 }
 
 cudaError_t nn_gelu_bwd(const void* pre, const void* dact, void* dpre, long n, cudaStream_t s) {
-  k_gelu_bwd<<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(pre), static_cast<const bf16*>(dact),
-                                         static_cast<bf16*>(dpre), n);
+  k_gelu_bwd<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(pre), static_cast<const bf16*>(dact),
+                                             static_cast<bf16*>(dpre), n / 8);
   return cudaGetLastError();
 }
 
 cudaError_t nn_pool2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s) {
   const long n = (long)N * H * W * C;
   if (backward)
-    k_pool2_bwd<<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
+    k_pool2_bwd<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
   else
-    k_pool2<<<grid_for(n / 4), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
+    k_pool2<<<grid_for(n / 32), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
   return cudaGetLastError();
 }
 
 cudaError_t nn_up2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s) {
   const long n = (long)N * H * W * C;
   if (backward)
-    k_up2_bwd<<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
+    k_up2_bwd<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
   else
-    k_up2<<<grid_for(4 * n), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
+    k_up2<<<grid_for(n / 2), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
   return cudaGetLastError();
 }
 
 cudaError_t nn_add(const void* a, const void* b, void* out, long n, cudaStream_t s) {
-  k_add<<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(a), static_cast<const bf16*>(b), static_cast<bf16*>(out),
-                                    n);
+  k_add<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(a), static_cast<const bf16*>(b),
+                                        static_cast<bf16*>(out), n / 8);
   return cudaGetLastError();
 }
 
@@ -513,6 +587,7 @@ int nn_done(cudaError_t e) {
 }
 
 bool aligned4(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) == 0; }
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 }  // namespace
 
@@ -535,36 +610,41 @@ int swe_nn_conv3x3_flip(const void* w, void* wf, int cin, int cout, void* stream
 int swe_nn_conv3x3_wgrad(const void* x, const void* dy, float* dw, float* db, int n, int h, int wd, int cin, int cout,
                          void* stream) {
   if (!x || !dy || !dw) return nn_fail(SWE_ERR_INVALID, "NULL tensor");
-  if (n < 1 || h < 1 || wd < 1 || cin < 16 || cin % 16 || cout < 8 || cout % 8)
-    return nn_fail(SWE_ERR_INVALID, "conv3x3_wgrad: need n, h, w >= 1, cin % 16 == 0, cout % 8 == 0");
+  if (n < 1 || h < 1 || wd < 1 || cin < 16 || cin % 16 || cout < 8 || cout % 8 || cout > 256)
+    return nn_fail(SWE_ERR_INVALID, "conv3x3_wgrad: need n, h, w >= 1, cin % 16 == 0, cout % 8 == 0, cout <= 256");
+  if (!aligned16(x) || !aligned16(dy)) return nn_fail(SWE_ERR_INVALID, "tensors must be 16-byte aligned");
   return nn_done(swe::nn_conv_wgrad(x, dy, dw, db, n, h, wd, cin, cout, static_cast<cudaStream_t>(stream)));
 }
 
 int swe_nn_gelu(const void* pre, void* act, int64_t count, void* stream) {
-  if (!pre || !act || count < 0) return nn_fail(SWE_ERR_INVALID, "gelu: bad arguments");
+  if (!pre || !act || count < 0 || count % 8 || !aligned16(pre) || !aligned16(act))
+    return nn_fail(SWE_ERR_INVALID, "gelu: need count % 8 == 0 and 16-byte aligned tensors");
   if (count == 0) return SWE_OK;
   return nn_done(swe::nn_gelu(pre, act, (long)count, static_cast<cudaStream_t>(stream)));
 }
 
 int swe_nn_gelu_bwd(const void* pre, const void* dact, void* dpre, int64_t count, void* stream) {
-  if (!pre || !dact || !dpre || count < 0) return nn_fail(SWE_ERR_INVALID, "gelu_bwd: bad arguments");
+  if (!pre || !dact || !dpre || count < 0 || count % 8 || !aligned16(pre) || !aligned16(dact) || !aligned16(dpre))
+    return nn_fail(SWE_ERR_INVALID, "gelu_bwd: need count % 8 == 0 and 16-byte aligned tensors");
   if (count == 0) return SWE_OK;
   return nn_done(swe::nn_gelu_bwd(pre, dact, dpre, (long)count, static_cast<cudaStream_t>(stream)));
 }
 
 int swe_nn_pool2(const void* x, void* y, int n, int h, int wd, int c, int backward, void* stream) {
-  if (!x || !y || n < 1 || h < 2 || wd < 2 || h % 2 || wd % 2 || c < 1)
-    return nn_fail(SWE_ERR_INVALID, "pool2: need even h, w >= 2");
+  if (!x || !y || n < 1 || h < 2 || wd < 2 || h % 2 || wd % 2 || c < 8 || c % 8 || !aligned16(x) || !aligned16(y))
+    return nn_fail(SWE_ERR_INVALID, "pool2: need even h, w >= 2, c % 8 == 0, 16-byte aligned tensors");
   return nn_done(swe::nn_pool2(x, y, n, h, wd, c, backward != 0, static_cast<cudaStream_t>(stream)));
 }
 
 int swe_nn_up2(const void* x, void* y, int n, int h, int wd, int c, int backward, void* stream) {
-  if (!x || !y || n < 1 || h < 1 || wd < 1 || c < 1) return nn_fail(SWE_ERR_INVALID, "up2: bad arguments");
+  if (!x || !y || n < 1 || h < 1 || wd < 1 || c < 8 || c % 8 || !aligned16(x) || !aligned16(y))
+    return nn_fail(SWE_ERR_INVALID, "up2: need c % 8 == 0 and 16-byte aligned tensors");
   return nn_done(swe::nn_up2(x, y, n, h, wd, c, backward != 0, static_cast<cudaStream_t>(stream)));
 }
 
 int swe_nn_add(const void* a, const void* b, void* out, int64_t count, void* stream) {
-  if (!a || !b || !out || count < 0) return nn_fail(SWE_ERR_INVALID, "add: bad arguments");
+  if (!a || !b || !out || count < 0 || count % 8 || !aligned16(a) || !aligned16(b) || !aligned16(out))
+    return nn_fail(SWE_ERR_INVALID, "add: need count % 8 == 0 and 16-byte aligned tensors");
   if (count == 0) return SWE_OK;
   return nn_done(swe::nn_add(a, b, out, (long)count, static_cast<cudaStream_t>(stream)));
 }
