@@ -69,7 +69,8 @@ def parse_args():
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
     ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
     ap.add_argument("--pairs", type=int, default=1024, help="surrogate: training pairs")
-    ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed Adam steps (batch 64)")
+    ap.add_argument("--train-steps", type=int, default=1000, help="surrogate: timed Adam steps")
+    ap.add_argument("--sur-batch", type=int, default=64, help="surrogate: training batch")
     ap.add_argument("--exact-size", type=int, default=256, help="exact-ensemble: map side")
     ap.add_argument("--cpu-sample", type=int, default=196608, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
@@ -714,7 +715,7 @@ def run_surrogate(args):
         return
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
-    size, cycles, particles, batch = 256, 50, 1000, 64
+    size, cycles, particles, batch = 256, 50, 1000, args.sur_batch
     t0 = time.perf_counter()
     h_tr, w_tr, d_tr = S.make_pairs(args.pairs, size, cycles, particles, seed=21)
     h_te, w_te, d_te = S.make_pairs(64, size, cycles, particles, seed=22)
@@ -814,7 +815,7 @@ def run_surrogate(args):
         "dtype": "bf16 (fp32 accumulate)",
         "data": "synthetic",
         "config": {"workload": f"U-Net 32/64/96/128 at 256^2, {args.pairs} training pairs of 50 cycles x 1000 "
-                               f"particles (PARALLEL plain method), batch 64, Adam lr 1e-3, "
+                               f"particles (PARALLEL plain method), batch {batch}, Adam lr 1e-3, "
                                f"{args.train_steps} timed steps",
                    "pairs": args.pairs, "pair_generation_s": gen_s, "l2": "activations of a batch exceed L2"},
         "surrogate": {"jump_ms": sur_ms, "jump_ms_per_terrain_batch64": sur_batch_ms, "plain_jump_ms": plain_ms,
