@@ -167,75 +167,94 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t& r0, uint32_t& r1, uint32
 }
 
 // dW[co][tap][ci] += sum_p dy[p][co] x[p + off(tap)][ci] (zero padding).
-// As a GEMM: rows co, columns ci, K = pixels. Each stage copies 32 pixels
-// of dy (32 channels from co0) and of the tap-shifted x (32 channels from
-// ci0) into shared memory, rows = pixels, with 16-byte loads; ldmatrix
-// .trans then hands out the fragments (A = dy^T, B = x, both with pixel
-// pairs per register). Channels past cout / cin and pixels past the map or
-// the batch are zero. The block's 32 x 32 partial sums go to dw with fp32
-// atomics. Requires cin % 8 == 0 and cout % 8 == 0.
+// As a GEMM per tap: rows co, columns ci, K = pixels. One block covers all
+// nine taps of a 32 x 32 (co, ci) tile, so a pixel chunk is read once per
+// block: each stage copies 32 pixels of dy (32 channels from co0) and, for
+// every tap, the 32 tap-shifted pixels of x (32 channels from ci0) into
+// shared memory, rows = pixels, with 16-byte loads (the nine shifted copies
+// overlap, so most of their reads hit L1); ldmatrix .trans then hands out
+// the fragments (A = dy^T, B = x, both with pixel pairs per register).
+// Channels past cout / cin and pixels past the map or the batch are zero.
+// The block's 9 x 32 x 32 partial sums go to dw with fp32 atomics. Requires
+// cin % 8 == 0 and cout % 8 == 0.
 __global__ void __launch_bounds__(128) k_conv_wgrad(const bf16* __restrict__ x, const bf16* __restrict__ dy,
                                                     float* __restrict__ dw, int N, int H, int W, int cin, int cout) {
   __shared__ __align__(16) bf16 sdy[kWgPix * kWgStride];
-  __shared__ __align__(16) bf16 sx[kWgPix * kWgStride];
+  __shared__ __align__(16) bf16 sx[9 * kWgPix * kWgStride];
   const long M = (long)N * H * W;
   const int ctile = (cin + kWgTile - 1) / kWgTile;
-  int by = blockIdx.y;
-  const int tap = by % 9;
-  by /= 9;
-  const int ci0 = (by % ctile) * kWgTile;
-  const int co0 = (by / ctile) * kWgTile;
-  const int ddy = tap / 3 - 1, ddx = tap % 3 - 1;
+  const int ci0 = (blockIdx.y % ctile) * kWgTile;
+  const int co0 = (blockIdx.y / ctile) * kWgTile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp >> 1) * 16, wn = (warp & 1) * 16;  // the warp's co / ci offsets in the tile
   // staging: thread -> (pixel row, 8-channel segment)
   const int srow = tid >> 2, sseg = (tid & 3) * 8;
-  float acc[2][4];
+  float acc[9][2][4];
 #pragma unroll
-  for (int j = 0; j < 2; j++)
+  for (int tp = 0; tp < 9; tp++)
 #pragma unroll
-    for (int q = 0; q < 4; q++) acc[j][q] = 0.0f;
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[tp][j][q] = 0.0f;
 
   const long pbeg = (long)blockIdx.x * kWgChunk;
   const long pend = pbeg + kWgChunk < M ? pbeg + kWgChunk : M;
   for (long p0 = pbeg; p0 < pend; p0 += kWgPix) {
     const long p = p0 + srow;
-    uint4 vdy = make_uint4(0, 0, 0, 0), vx = make_uint4(0, 0, 0, 0);
+    uint4 vdy = make_uint4(0, 0, 0, 0);
+    uint4 vx[9];
+    int px = 0, py = 0;
     if (p < pend) {
       if (co0 + sseg < cout) vdy = *reinterpret_cast<const uint4*>(dy + p * cout + co0 + sseg);
-      const int xx = (int)(p % W) + ddx, yy = (int)((p / W) % H) + ddy;
-      if (ci0 + sseg < cin && xx >= 0 && xx < W && yy >= 0 && yy < H)
-        vx = *reinterpret_cast<const uint4*>(x + (p + (long)ddy * W + ddx) * cin + ci0 + sseg);
+      px = (int)(p % W);
+      py = (int)((p / W) % H);
+    }
+#pragma unroll
+    for (int tp = 0; tp < 9; tp++) {
+      const int ddy = tp / 3 - 1, ddx = tp % 3 - 1;
+      const int xx = px + ddx, yy = py + ddy;
+      vx[tp] = make_uint4(0, 0, 0, 0);
+      if (p < pend && ci0 + sseg < cin && xx >= 0 && xx < W && yy >= 0 && yy < H)
+        vx[tp] = *reinterpret_cast<const uint4*>(x + (p + (long)ddy * W + ddx) * cin + ci0 + sseg);
     }
     __syncthreads();  // the previous stage's fragments are read
     *reinterpret_cast<uint4*>(sdy + srow * kWgStride + sseg) = vdy;
-    *reinterpret_cast<uint4*>(sx + srow * kWgStride + sseg) = vx;
+#pragma unroll
+    for (int tp = 0; tp < 9; tp++)
+      *reinterpret_cast<uint4*>(sx + (tp * kWgPix + srow) * kWgStride + sseg) = vx[tp];
     __syncthreads();
+    const int mi = lane >> 3, r = lane & 7;
 #pragma unroll
     for (int k0 = 0; k0 < kWgPix; k0 += 16) {
       // A (16 co x 16 px): matrices (co 0-7 | 8-15) x (px 0-7 | 8-15)
-      const int mi = lane >> 3, r = lane & 7;
-      uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
+      uint32_t a0, a1, a2, a3;
       ldsm_x4_trans(a0, a1, a2, a3, sdy + (k0 + r + ((mi >> 1) << 3)) * kWgStride + wm + ((mi & 1) << 3));
-      // B (16 px x 16 ci): matrices (px 0-7 | 8-15) x (ci 0-7 | 8-15)
-      ldsm_x4_trans(b0, b1, b2, b3, sx + (k0 + r + ((mi & 1) << 3)) * kWgStride + wn + ((mi >> 1) << 3));
-      mma16816(acc[0], a0, a1, a2, a3, b0, b1);
-      mma16816(acc[1], a0, a1, a2, a3, b2, b3);
+#pragma unroll
+      for (int tp = 0; tp < 9; tp++) {
+        // B (16 px x 16 ci): matrices (px 0-7 | 8-15) x (ci 0-7 | 8-15)
+        uint32_t b0, b1, b2, b3;
+        ldsm_x4_trans(b0, b1, b2, b3,
+                      sx + (tp * kWgPix + k0 + r + ((mi & 1) << 3)) * kWgStride + wn + ((mi >> 1) << 3));
+        mma16816(acc[tp][0], a0, a1, a2, a3, b0, b1);
+        mma16816(acc[tp][1], a0, a1, a2, a3, b2, b3);
+      }
     }
   }
   const int g = lane >> 2, t = lane & 3;
 #pragma unroll
-  for (int j = 0; j < 2; j++) {
-    const int ci = ci0 + wn + 8 * j + 2 * t;
+  for (int tp = 0; tp < 9; tp++)
 #pragma unroll
-    for (int r2 = 0; r2 < 2; r2++) {
-      const int co = co0 + wm + g + 8 * r2;
-      if (co >= cout || ci >= cin) continue;
-      float* o = dw + ((long)co * 9 + tap) * cin + ci;
-      atomicAdd(o, acc[j][2 * r2]);
-      atomicAdd(o + 1, acc[j][2 * r2 + 1]);
+    for (int j = 0; j < 2; j++) {
+      const int ci = ci0 + wn + 8 * j + 2 * t;
+#pragma unroll
+      for (int r2 = 0; r2 < 2; r2++) {
+        const int co = co0 + wm + g + 8 * r2;
+        if (co >= cout || ci >= cin) continue;
+        float* o = dw + ((long)co * 9 + tp) * cin + ci;
+        atomicAdd(o, acc[tp][j][2 * r2]);
+        atomicAdd(o + 1, acc[tp][j][2 * r2 + 1]);
+      }
     }
-  }
 }
 
 // db[co] += sum_p dy[p][co]. Thread -> (pixel row, 8-channel group) with
@@ -490,7 +509,7 @@ cudaError_t nn_conv_wgrad(const void* x, const void* dy, float* dw, float* db, i
                           cudaStream_t s) {
   const long M = (long)N * H * W;
   const long chunks = (M + kWgChunk - 1) / kWgChunk;
-  const int tiles = 9 * ((cin + kWgTile - 1) / kWgTile) * ((cout + kWgTile - 1) / kWgTile);
+  const int tiles = ((cin + kWgTile - 1) / kWgTile) * ((cout + kWgTile - 1) / kWgTile);
   if (chunks > 0x7fffffffL || tiles > 65535) return cudaErrorInvalidValue;
   k_conv_wgrad<<<dim3((unsigned)chunks, (unsigned)tiles), 128, 0, s>>>(static_cast<const bf16*>(x),
                                                                       static_cast<const bf16*>(dy), dw, N, H, W, cin,
