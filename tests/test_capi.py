@@ -86,3 +86,39 @@ def test_batch_rejects_bad_arguments(lib_built):
     assert L.swe_batch_erode_ordered(None, -1, 1, None) == -1
     assert L.swe_batch_erode_ordered(None, 2, 1, None) == -1
     assert L.swe_batch_erode_ordered(None, 0, 1, None) == 0
+
+
+def test_surrogate_entry_points_reject_bad_arguments(lib_built):
+    # argument checks run before any device work, so no GPU is needed
+    import ctypes
+    L = swe.lib
+    P = ctypes.c_void_p
+    fake = P(0x1000)  # never dereferenced: every call below fails its checks first
+    odd = P(0x1002)
+    L.swe_nn_conv3x3.argtypes = [P, P, P, P] + [ctypes.c_int] * 5 + [P]
+    assert L.swe_nn_conv3x3(None, fake, None, fake, 1, 8, 8, 16, 16, None) == -1      # NULL input
+    assert L.swe_nn_conv3x3(fake, fake, None, fake, 1, 8, 8, 12, 16, None) == -1      # cin % 16
+    assert L.swe_nn_conv3x3(fake, fake, None, fake, 1, 8, 8, 16, 12, None) == -1      # cout % 8
+    assert L.swe_nn_conv3x3(odd, fake, None, fake, 1, 8, 8, 16, 16, None) == -1       # alignment
+    L.swe_nn_conv3x3_wgrad.argtypes = [P, P, P, P] + [ctypes.c_int] * 5 + [P]
+    assert L.swe_nn_conv3x3_wgrad(fake, fake, fake, None, 1, 8, 8, 16, 264, None) == -1  # cout > 256
+    L.swe_nn_pool2.argtypes = [P, P] + [ctypes.c_int] * 5 + [P]
+    assert L.swe_nn_pool2(fake, fake, 1, 7, 8, 16, 0, None) == -1                     # odd height
+    assert L.swe_nn_pool2(fake, fake, 1, 8, 8, 12, 0, None) == -1                     # c % 8
+    L.swe_nn_gelu.argtypes = [P, P, ctypes.c_int64, P]
+    assert L.swe_nn_gelu(fake, fake, 12, None) == -1                                  # count % 8
+    assert L.swe_nn_gelu(fake, fake, 0, None) == 0                                    # nothing to do
+    L.swe_nn_adam.argtypes = [P, P, P, P, P, ctypes.c_int64] + [ctypes.c_float] * 4 + [ctypes.c_int, P]
+    assert L.swe_nn_adam(fake, fake, fake, fake, None, 8, 1e-3, 0.9, 0.999, 1e-8, 0, None) == -1  # step 0
+    assert b"adam" in L.swe_last_error()
+
+
+def test_surrogate_flop_count():
+    from simplewinderosion_gb300 import surrogate
+    fwd = surrogate.conv_flops(1, 8, 8)
+    # by hand: 2 * cin * cout * 9 * pixels of each layer's resolution
+    want = 2 * 9 * (16 * 32 * 64 + 32 * 32 * 64 + 32 * 64 * 16 + 64 * 96 * 4 + 96 * 128 * 1 + 128 * 128 * 1
+                    + 128 * 96 * 4 + 96 * 64 * 16 + 64 * 32 * 64 + 32 * 16 * 64)
+    assert fwd == want
+    # a training step adds the input gradients (all but the first layer) and the weight gradients
+    assert surrogate.conv_flops(1, 8, 8, backward=True) == 3 * want - 2 * 9 * 16 * 32 * 64
