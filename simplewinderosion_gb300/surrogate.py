@@ -344,13 +344,16 @@ class Rollout:
     run over every `judge_every`-th jump as correction and judge. A jump whose
     prediction misses the plain result by more than `bound` (height RMSE
     relative to the plain result's height range) rejects the surrogate: it
-    and every later jump use the plain method."""
+    and every later jump use the plain method. `world` (default: a new World
+    of the given size, wind and seed) is the terrain's holder and the plain
+    method's runner."""
 
-    def __init__(self, model: Surrogate, size, wind, cycles=50, particles=1000, seed=1, judge_every=4, bound=0.01):
+    def __init__(self, model: Surrogate, size, wind, cycles=50, particles=1000, seed=1, judge_every=4, bound=0.01,
+                 world=None):
         self.model, self.size, self.cycles, self.particles = model, size, cycles, particles
         self.wind = wind_direction(*wind)
         self.judge_every, self.bound = judge_every, bound
-        self.world = World(size, params=Params(pspeed=self.wind), seed=seed)
+        self.world = world if world is not None else World(size, params=Params(pspeed=self.wind), seed=seed)
         self.rejected = False
         self.jumps = 0
         self.judged = []  # relative RMSE of each judged jump
@@ -358,16 +361,19 @@ class Rollout:
     def start(self, height):
         self.world.upload(Field.HEIGHT, np.asarray(height, np.float32))
 
-    def step(self):
+    def predict_change(self, h):
+        """The surrogate's height change over one jump, for the map h."""
         torch = self.model.torch
+        hd = torch.from_numpy(np.ascontiguousarray(h[None], dtype=np.float32)).to(self.model.device)
+        wd = torch.tensor([[self.wind[0], self.wind[2]]], dtype=torch.float32, device=self.model.device)
+        return self.model.predict(hd, wd)[0].cpu().numpy()
+
+    def step(self):
+        """One jump; returns the terrain after it."""
         h = self.world.height
         self.jumps += 1
         judge = self.rejected or self.jumps % self.judge_every == 0
-        pred = None
-        if not self.rejected:
-            hd = torch.from_numpy(h[None]).to(self.model.device)
-            wd = torch.tensor([[self.wind[0], self.wind[2]]], dtype=torch.float32, device=self.model.device)
-            pred = h + self.model.predict(hd, wd)[0].cpu().numpy()
+        pred = None if self.rejected else h + self.predict_change(h)
         if judge:
             self.world.erode(self.particles, self.cycles, mode=Mode.PARALLEL)
             plain = self.world.height
