@@ -319,8 +319,8 @@ int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, const swe_p
  * the terrain after a number of erode cycles, trained on pairs the erosion
  * path produces, with that path as its fallback and judge). Tensors are
  * device arrays in NHWC order (channels innermost); "bf16" tensors hold
- * bfloat16 values (uint16 storage) and must be 4-byte aligned; arithmetic
- * accumulates in fp32. Every call is enqueued on `stream` (NULL: the default
+ * bfloat16 values (uint16 storage) and must be 16-byte aligned (the
+ * convolution's output: 4-byte); arithmetic accumulates in fp32. Every call is enqueued on `stream` (NULL: the default
  * stream) and returns once enqueued.
  *
  * y[n,i,j,co] = bias[co] + sum over the 3x3 taps (zero padding) and ci of

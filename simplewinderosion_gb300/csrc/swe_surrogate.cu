@@ -617,7 +617,8 @@ int swe_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int
   if (!x || !w || !y) return nn_fail(SWE_ERR_INVALID, "NULL tensor");
   if (n < 1 || h < 1 || wd < 1 || cin < 16 || cin % 16 || cout < 8 || cout % 8)
     return nn_fail(SWE_ERR_INVALID, "conv3x3: need n, h, w >= 1, cin % 16 == 0, cout % 8 == 0");
-  if (!aligned4(x) || !aligned4(w) || !aligned4(y)) return nn_fail(SWE_ERR_INVALID, "tensors must be 4-byte aligned");
+  if (!aligned16(x) || !aligned16(w) || !aligned4(y))
+    return nn_fail(SWE_ERR_INVALID, "x and w must be 16-byte aligned, y 4-byte aligned");
   return nn_done(swe::nn_conv3x3(x, w, bias, y, n, h, wd, cin, cout, static_cast<cudaStream_t>(stream)));
 }
 
