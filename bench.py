@@ -203,7 +203,37 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- CPU legs
 def cpu_cores_desc() -> str:
-    return f"{platform.machine()} x{os.cpu_count()}"
+    core = pinned_core()
+    return f"{platform.machine()} x{os.cpu_count()}" + (f", pinned to core {core}" if core is not None else "")
+
+
+def pinned_core():
+    """The host core the single-threaded CPU samples run on: the highest one
+    this process may use (None where affinity cannot be set)."""
+    try:
+        return max(os.sched_getaffinity(0))
+    except (AttributeError, OSError, ValueError):
+        return None
+
+
+class _PinnedToOneCore:
+    """Runs a block on one host core, then restores the process's affinity."""
+
+    def __enter__(self):
+        self.saved = None
+        core = pinned_core()
+        if core is not None:
+            try:
+                self.saved = os.sched_getaffinity(0)
+                os.sched_setaffinity(0, {core})
+            except OSError:
+                self.saved = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.saved is not None:
+            os.sched_setaffinity(0, self.saved)
+        return False
 
 
 def cpu_sample(size: int, h, wind, particles: int, total_particles: int, prefer_reference: bool):
@@ -222,17 +252,19 @@ def cpu_sample(size: int, h, wind, particles: int, total_particles: int, prefer_
         ref = oracle.Reference(size)
         ref.reset(h)
         ref.srand(1)
-        t0 = time.perf_counter()
-        ref.erode(particles, 1, pspeed=wind)
-        dt = time.perf_counter() - t0
+        with _PinnedToOneCore():
+            t0 = time.perf_counter()
+            ref.erode(particles, 1, pspeed=wind)
+            dt = time.perf_counter() - t0
         steps = None
     else:
         port = oracle.Port(size, pspeed=wind)
         port.set_field(0, h)
         port.seed(1)
-        t0 = time.perf_counter()
-        port.erode(particles, 1)
-        dt = time.perf_counter() - t0
+        with _PinnedToOneCore():
+            t0 = time.perf_counter()
+            port.erode(particles, 1)
+            dt = time.perf_counter() - t0
         steps = port.stats()[0]
     cycles_per_s = particles / (dt * total_particles)
     return cycles_per_s, kind, dt, steps
@@ -654,9 +686,10 @@ def run_exact_ensemble(args):
         port = oracle.Port(size, pspeed=wind)
         port.set_field(0, h0)
         port.seed(1)
-        t0 = time.perf_counter()
-        port.erode(particles, 100)
-        cpu_s = time.perf_counter() - t0
+        with _PinnedToOneCore():
+            t0 = time.perf_counter()
+            port.erode(particles, 100)
+            cpu_s = time.perf_counter() - t0
         cpu = {"value": port.stats()[0] / cpu_s, "unit": "particle-steps/s", "cores": 1, "kind": "port",
                "sample": f"one run (100 cycles x 1000 particles) of world 0 on {cpu_cores_desc()}, "
                          f"one thread ({cpu_s:.1f} s)"}
