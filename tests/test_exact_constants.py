@@ -70,3 +70,45 @@ def test_drag_split_of_double_point_three():
     assert dhi == nearest_f32(d) and dlo == nearest_f32(d - Decimal(dhi))
     assert abs(d - Decimal(dhi) - Decimal(dlo)) < Decimal(2) ** -52
     assert "0x3e99999au" in SRC and "0xb24ccccdu" in SRC
+
+
+def _drag_fast(s):
+    """drag_factor's float-float path (csrc/swe_device.cuh) in numpy float32:
+    returns (accepted mask, value). The one fused multiply-add is exact here:
+    s * Dhi is exact in double, and so is its difference from its float
+    rounding, so rounding that difference to float is the fmaf result."""
+    f32, f64 = np.float32, np.float64
+    dhi, dlo = f32(np.uint32(0x3E99999A).view(np.float32)), f32(np.uint32(0xB24CCCCD).view(np.float32))
+    s = s.astype(np.float32)
+    p1 = s * dhi
+    e1 = (s.astype(f64) * f64(dhi) - p1.astype(f64)).astype(np.float32)
+    p2 = s * dlo
+    one = np.float32(1.0)
+    a = one + (-p1)                          # two_sum(1, -p1)
+    bb = a - one
+    b = (one - (a - bb)) + ((-p1) - bb)
+    b = (b - e1) - p2
+    hi = a + b                               # fast_two_sum(a, b)
+    lo = b - (hi - a)
+    bits = hi.view(np.uint32)
+    up = (bits + np.uint32(1)).view(np.float32) - hi
+    down = hi - (bits - np.uint32(1)).view(np.float32)
+    u = np.where(lo < 0, down, up)
+    ok = np.abs(lo) <= np.float32(0.499) * u
+    return ok, hi
+
+
+def test_drag_fast_path_equals_the_double_expression():
+    rs = np.random.RandomState(0)
+    s = np.concatenate([rs.uniform(0.0, 2.0, 1_000_000).astype(np.float32),
+                        np.asarray([0.0, 2 ** -149, 1e-30, 0.5, 1.0, 1.5, np.nextafter(np.float32(2.0), 0)],
+                                   np.float32),
+                        (np.arange(1, 100_001, dtype=np.float32) * np.float32(2.0 ** -16))])
+    ok, fast = _drag_fast(s)
+    want = (1.0 - 0.3 * s.astype(np.float64)).astype(np.float32)
+    assert np.array_equal(fast[ok].view(np.uint32), want[ok].view(np.uint32))
+    # The rest (about 3 % here) take the double expression: a float s in
+    # [2^-k, 2^(1-k)) is a multiple of 2^-(23+k), so 1 - 0.3 s often lands a
+    # tenth of an ulp grid away from a rounding midpoint by 1e-17 or less, a
+    # tie that only the double expression's own roundings decide.
+    assert ok.mean() > 0.95
