@@ -73,7 +73,8 @@ def parse_args():
     ap.add_argument("--sur-batch", type=int, default=64, help="surrogate: training batch")
     ap.add_argument("--exact-size", type=int, default=256, help="exact-ensemble: map side")
     ap.add_argument("--cpu-sample", type=int, default=196608, help="particles in the CPU baseline sample")
-    ap.add_argument("--ref-sample", type=int, default=16384, help="particles per reference-arm step")
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="particles per reference-arm step (default: a tenth of a cycle)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -252,11 +253,15 @@ def cpu_sample(size: int, h, wind, particles: int, total_particles: int, prefer_
         ref = oracle.Reference(size)
         ref.reset(h)
         ref.srand(1)
+        calls0 = ref.L.ref_rand_calls()
         with _PinnedToOneCore():
             t0 = time.perf_counter()
             ref.erode(particles, 1, pspeed=wind)
             dt = time.perf_counter() - t0
-        steps = None
+        # 4 rand() calls per spawn (world.hpp:52-54) and 3 per particle-step
+        # (the turbulence draw, wind.hpp:83, made on every step that passes
+        # the age and map checks)
+        steps = (ref.L.ref_rand_calls() - calls0 - 4 * particles) // 3
     else:
         port = oracle.Port(size, pspeed=wind)
         port.set_field(0, h)
@@ -270,6 +275,11 @@ def cpu_sample(size: int, h, wind, particles: int, total_particles: int, prefer_
     return cycles_per_s, kind, dt, steps
 
 
+def cpu_work(sample: int, dt: float, steps) -> dict:
+    """Per-particle work of a CPU sample, to set beside the GPU cycle's."""
+    return {"steps_per_particle": steps / sample, "particle_steps_per_s": steps / dt} if steps else {}
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
@@ -278,14 +288,18 @@ def run_reference(args):
     size = args.size
     particles = args.particles or size * size
     h, wind = workload(size)
-    sample = args.ref_sample
-    vals, secs, kind = [], [], "port"
+    sample = args.ref_sample or max(1, particles // 10)
+    vals, secs, steps, kind = [], [], [], "port"
+    # every step: the first `sample` particles of the first cycle on the
+    # initial terrain (the same work as every timed GPU cycle's start)
     for i in range(args.warmup + args.steps):
-        v, kind, dt, _ = cpu_sample(size, h, wind, sample, particles, prefer_reference=True)
+        v, kind, dt, st = cpu_sample(size, h, wind, sample, particles, prefer_reference=True)
         if i >= args.warmup:
             vals.append(v)
             secs.append(dt)
+            steps.append(st or 0)
     value = statistics.mean(vals)
+    step_s = statistics.mean(secs)
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -294,7 +308,8 @@ def run_reference(args):
         "n_gpus": args.gpus,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 / value,
+        "ms_per_step": 1e3 * step_s,
+        "cycles_per_step": sample / particles,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -303,8 +318,10 @@ def run_reference(args):
         "config": config_dict(args, particles),
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": 1, "kind": kind,
-            "sample": f"{sample} of {particles} particles of one sequential World::erode cycle per step on "
-                      f"{cpu_cores_desc()} (the reference loop is single-threaded), scaled to cycles/s",
+            "sample": f"each step: the first {sample} of the {particles} particles ({100 * sample / particles:.0f} %) "
+                      f"of one sequential World::erode cycle on the initial terrain, on {cpu_cores_desc()} (the "
+                      f"reference loop is single-threaded), scaled to cycles/s",
+            **cpu_work(sample * len(secs), sum(secs), sum(steps)),
         },
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -339,6 +356,7 @@ def run_ours(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     for _ in range(args.warmup):
+        w.upload(swe.Field.HEIGHT, h)
         w.erode(particles, 1, mode=swe.Mode.PARALLEL)
     torch.cuda.synchronize()
 
@@ -352,6 +370,9 @@ def run_ours(args):
     fly_ms = cas_ms = 0.0
     psteps = transfers = 0
     for _ in range(args.steps):
+        # every timed cycle is a first cycle on the initial terrain, the work
+        # the CPU samples time (uploaded outside the timed region)
+        w.upload(swe.Field.HEIGHT, h)
         flush.zero_()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -421,7 +442,9 @@ def run_ours(args):
         "particle_steps_per_s": whole_job_rate(psteps, world_size, total_ms),
         "kernels": {"cycle_ms": ms_per_step, "fly_phases_ms": fly_ms / args.steps,
                     "cascade_phases_ms": cas_ms / args.steps, "k_transfers_per_step": k,
-                    "particle_steps_per_cycle": psteps_per_launch},
+                    "particle_steps_per_cycle": psteps_per_launch,
+                    "steps_per_particle": psteps_per_launch / particles},
+        "timed_cycles": "each a first cycle on the initial terrain (re-uploaded before it, outside the timing)",
         "roofline": {
             "bound": "hbm",
             "kernel": kernel_name,
@@ -438,7 +461,7 @@ def run_ours(args):
     }
 
     if not args.no_e2e:
-        line["e2e"] = e2e(w, swe, torch, stream, particles, args, world_size)
+        line["e2e"] = e2e(w, swe, torch, stream, particles, args, world_size, h)
 
     if not args.no_all_at_once and args.lanes >= 0:
         line["all_at_once"] = all_at_once(swe, torch, dev, h, wind, particles, args, world_size, rank)
@@ -447,9 +470,10 @@ def run_ours(args):
         v, kind, dt, steps = cpu_sample(size, h, wind, args.cpu_sample, particles, prefer_reference=True)
         line["cpu_baseline"] = {
             "value": v, "unit": UNIT, "cores": 1, "kind": kind,
-            "sample": f"{args.cpu_sample} of {particles} particles of one sequential World::erode cycle "
-                      f"({dt:.1f} s on {cpu_cores_desc()}, one thread: the reference loop is sequential), "
-                      f"scaled to cycles/s",
+            "sample": f"the first {args.cpu_sample} of the {particles} particles of one sequential World::erode "
+                      f"cycle on the initial terrain ({dt:.1f} s on {cpu_cores_desc()}, one thread: the reference "
+                      f"loop is sequential), scaled to cycles/s",
+            **cpu_work(args.cpu_sample, dt, steps),
         }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -492,20 +516,19 @@ def all_at_once(swe, torch, dev, h, wind, particles, args, world_size, rank):
                     "histogram and spectrum drift from the sequential reference's (not the headline)"}
 
 
-def e2e(w, swe, torch, stream, particles, args, world_size):
+def e2e(w, swe, torch, stream, particles, args, world_size, h):
     """Cycles/s through the C ABI with the height map kept on the host: per
     cycle, upload the height map from pinned memory, erode one cycle, read
     back height and momentum (the fields the reference's app loop reads after
-    erode, SimpleWindErosion.cpp:217-230). Each cycle uploads the height the
-    previous one read back (Q16.16 heights round-trip through float exactly),
-    so these cycles continue the trajectory the device-timed cycles were on,
-    at the same per-cycle cost; the copies replace the L2 flush."""
+    erode, SimpleWindErosion.cpp:217-230). Every cycle uploads the initial
+    terrain, so each is the same first-cycle work the device-timed cycles and
+    the CPU samples do; the copies replace the L2 flush."""
     import torch.distributed as dist
     n = w.n
-    h_pin = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_pin = torch.from_numpy(np.ascontiguousarray(h, np.float32).reshape(-1)).pin_memory()
+    out_pin = torch.empty(n, dtype=torch.float32).pin_memory()
     moms = [torch.empty(n, dtype=torch.float32).pin_memory() for _ in range(3)]
     mom_fields = [swe.Field.MOMENTUMX, swe.Field.MOMENTUMY, swe.Field.MOMENTUMZ]
-    w.download_ptr(swe.Field.HEIGHT, h_pin.data_ptr(), n)
     torch.cuda.synchronize()
     if world_size > 1:
         dist.barrier()
@@ -516,7 +539,7 @@ def e2e(w, swe, torch, stream, particles, args, world_size):
         e0.record(stream)
         w.upload_ptr(swe.Field.HEIGHT, h_pin.data_ptr(), n)
         w.erode(particles, 1, mode=swe.Mode.PARALLEL, sync=False)
-        w.download_ptr(swe.Field.HEIGHT, h_pin.data_ptr(), n)
+        w.download_ptr(swe.Field.HEIGHT, out_pin.data_ptr(), n)
         for f, o in zip(mom_fields, moms):
             w.download_ptr(f, o.data_ptr(), n)
         e1.record(stream)

@@ -169,6 +169,15 @@ int swe_world_erode(swe_world* w, int cycles, int particles_per_cycle, swe_mode 
 int swe_world_get_cycle(swe_world* w, uint64_t* cycle);
 int swe_world_set_cycle(swe_world* w, uint64_t cycle);
 
+/* Deadline of every wait inside a PARALLEL cycle (a grid barrier, a cell
+ * tag), in nanoseconds; 0 restores the default of 2 s. A wait that runs past
+ * it sets SWE_STATUS_TIMEOUT, every thread of the cycle leaves at the same
+ * barrier, and the next swe_world_sync reports SWE_ERR_DEVICE; the world's
+ * maps then hold a partly run cycle (upload fresh fields to go on). No
+ * counterpart in the reference (its loop never waits): it exists so the
+ * abort path can be exercised on a normal, terminating workload. */
+int swe_world_set_wait_limit(swe_world* w, uint64_t ns);
+
 /* An ensemble: `cycles` PARALLEL erode cycles of worlds[i] with
  * particles_per_cycle[i] particles each, for `count` independent worlds
  * (sizes, seeds, winds and parameters of their own). Each world's result is
@@ -181,6 +190,36 @@ int swe_world_set_cycle(swe_world* w, uint64_t cycle);
  * asynchronous on their streams); not for stream capture. Extends the reference, which erodes one
  * world (world.hpp:36-77). */
 int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle);
+
+/* A prepared ensemble for repeated runs and CUDA-graph capture: the same
+ * computation as swe_batch_erode (each world ends as swe_world_erode would
+ * leave it), with the per-world launch entries written to the device once.
+ * Every world's particles in flight must fit one cluster (else
+ * SWE_ERR_INVALID); the worlds must outlive the batch. With tune != 0 the
+ * launch shape (CTAs per cluster 4/8/16 x threads per CTA 128/256; it
+ * changes no result) is chosen by timing one cycle of each feasible shape on
+ * scratch copies of the worlds, and cached for the process per batch
+ * signature (the sorted sides, particle counts and lanes of its worlds);
+ * tune == 0 takes 16 CTAs x 256 threads. No counterpart in the reference,
+ * which erodes one world (world.hpp:36-77). */
+typedef struct swe_batch swe_batch;
+int swe_batch_create(swe_world* const* worlds, int count, const int* particles_per_cycle, int tune, swe_batch** out);
+/* `cycles` PARALLEL erode cycles of every world of the batch, enqueued on the
+ * first world's stream (ordering with work on the other worlds' streams is
+ * the caller's). Enqueues memsets and one kernel launch only, so it can be
+ * captured into a CUDA graph on that stream; each replay runs `cycles` more
+ * cycles (the worlds' cycle counters live on the device). Heights uploaded
+ * after swe_batch_create are taken into fixed point by the next direct call,
+ * not by replays of a graph captured before the upload. */
+int swe_batch_run(swe_batch* b, int cycles);
+/* The launch shape in use; after tuning, the measured cycle time (ms) of the
+ * chosen shape and of the default shape (0 when not measured). */
+int swe_batch_shape(swe_batch* b, int* ctas_per_cluster, int* threads_per_cta, double* tuned_ms, double* default_ms);
+/* Sets the launch shape by hand (CTAs per cluster 4, 8 or 16; threads per
+ * CTA a multiple of 32 up to 256); SWE_ERR_INVALID if a world's particles in
+ * flight do not fit one cluster of it. */
+int swe_batch_set_shape(swe_batch* b, int ctas_per_cluster, int threads_per_cta);
+void swe_batch_destroy(swe_batch* b);
 
 /* An ensemble in ORDERED mode: `cycles` erode cycles of worlds[i] with
  * particles_per_cycle[i] particles each, every world bit for bit what
@@ -299,10 +338,11 @@ int swe_world_expf_bits(swe_world* w, uint32_t first_bits, size_t n, float* host
  * parallel erode cycles of `particles_per_cycle` particles (same results as a
  * world whose random-number cycle counter is `first_cycle`), enqueued on
  * `stream` (NULL: the default stream). The scratch it needs lives in one
- * static device array, about 21.6 MB on every GPU that loads the library,
+ * static device array, about 17.1 MiB on every GPU that loads the library,
  * held until the process exits; its limits are SWE_NOALLOC_MAX_CELLS cells
  * and SWE_NOALLOC_MAX_PARTICLES particles per cycle, and larger requests fail
- * with SWE_ERR_INVALID. The first call on a device looks up that array's
+ * with SWE_ERR_INVALID. Particles in flight stay in the kernel's shared
+ * memory (at most SMs x 1,024 of them; more are refused the same way). The first call on a device looks up that array's
  * device address (set-up, once per device): make that first call before any
  * stream capture. All calls share the array, so calls that overlap on the GPU
  * race; serialise them (one stream, or synchronise between them). If

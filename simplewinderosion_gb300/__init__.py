@@ -136,8 +136,17 @@ def _setup(L):
     L.swe_terrain_default.restype = None
     L.swe_world_get_cycle.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
     L.swe_world_set_cycle.argtypes = [_P, ctypes.c_uint64]
+    L.swe_world_set_wait_limit.argtypes = [_P, ctypes.c_uint64]
     L.swe_batch_erode.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.swe_batch_erode_ordered.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.swe_batch_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                   ctypes.POINTER(_P)]
+    L.swe_batch_run.argtypes = [_P, ctypes.c_int]
+    L.swe_batch_shape.argtypes = [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    L.swe_batch_set_shape.argtypes = [_P, ctypes.c_int, ctypes.c_int]
+    L.swe_batch_destroy.argtypes = [_P]
+    L.swe_batch_destroy.restype = None
     L.swe_world_sync.argtypes = [_P]
     L.swe_world_status.argtypes = [_P, ctypes.POINTER(ctypes.c_uint32)]
     L.swe_world_seed_rand.argtypes = [_P, ctypes.c_uint32]
@@ -373,6 +382,12 @@ class World:
     def cycle(self, value: int) -> None:
         _check(lib.swe_world_set_cycle(self._h, ctypes.c_uint64(int(value))))
 
+    def set_wait_limit(self, ns: int) -> None:
+        """Deadline (ns) of every wait inside a PARALLEL cycle; 0 restores
+        the default 2 s. A wait past it aborts the cycle with
+        SWE_STATUS_TIMEOUT (reported by the next sync)."""
+        _check(lib.swe_world_set_wait_limit(self._h, ctypes.c_uint64(int(ns))))
+
     def vertices(self) -> np.ndarray:
         """swe_world_vertices: [nx, nz, 12] floats per cell, the position,
         normal and +x/+z edge vectors updatenode writes for rendering."""
@@ -418,3 +433,43 @@ def batch_erode(worlds, cycles: int, particles, mode: Mode = Mode.PARALLEL) -> N
         _check(lib.swe_batch_erode_ordered(handles, len(worlds), int(cycles), counts))
     else:
         _check(lib.swe_batch_erode(handles, len(worlds), int(cycles), counts))
+
+
+class Batch:
+    """A prepared PARALLEL ensemble (swe_batch_create): repeated runs in one
+    persistent launch each, capturable into a CUDA graph; `tune` picks the
+    launch shape by measurement. The worlds must outlive the batch."""
+
+    def __init__(self, worlds, particles, tune: bool = False):
+        self.worlds = list(worlds)
+        if isinstance(particles, int):
+            particles = [particles] * len(self.worlds)
+        handles = (_P * len(self.worlds))(*[w._h for w in self.worlds])
+        counts = (ctypes.c_int * len(self.worlds))(*[int(p) for p in particles])
+        self._h = _P()
+        _check(lib.swe_batch_create(handles, len(self.worlds), counts, 1 if tune else 0, ctypes.byref(self._h)))
+
+    def run(self, cycles: int = 1) -> None:
+        """Enqueue `cycles` cycles on the first world's stream."""
+        _check(lib.swe_batch_run(self._h, int(cycles)))
+
+    def shape(self) -> dict:
+        c, t, tm, dm = ctypes.c_int(), ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        _check(lib.swe_batch_shape(self._h, ctypes.byref(c), ctypes.byref(t), ctypes.byref(tm), ctypes.byref(dm)))
+        return {"ctas_per_cluster": c.value, "threads_per_cta": t.value, "tuned_ms": tm.value,
+                "default_ms": dm.value}
+
+    def set_shape(self, ctas: int, threads: int) -> None:
+        _check(lib.swe_batch_set_shape(self._h, int(ctas), int(threads)))
+
+    def close(self):
+        if self._h:
+            lib.swe_batch_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include <cstdio>
 #include <cstring>
@@ -110,6 +112,11 @@ struct swe_world {
   uint32_t* expf_x = nullptr;  // device copy of the expf exception list
   int8_t* expf_d = nullptr;
   int expf_n = 0;
+  uint64_t wait_ns = 0;  // parallel-mode wait deadline (0: the default, 2 s)
+  // An aborted parallel cycle (SWE_STATUS_TIMEOUT) leaves deltas and visit
+  // counts behind in maps that every cycle expects at zero; the next
+  // parallel call clears them first.
+  bool scratch_dirty = false;
 
   Consts consts() const {
     Consts c;
@@ -124,6 +131,7 @@ struct swe_world {
     c.expf_x = expf_x;
     c.expf_d = expf_d;
     c.expf_n = expf_n;
+    c.wait_ns = wait_ns;
     return c;
   }
 
@@ -198,6 +206,16 @@ int ensure_fixed(swe_world* w) {
   swe::launch_height_to_fixed(w->F.f[0], w->pb.hq, c, w->cnt, w->stream);
   SWE_CK(cudaGetLastError());
   w->hq_valid = true;
+  return SWE_OK;
+}
+
+// After an aborted cycle: zero the deltas and visit counts of even and odd
+// steps (the maps after the heights), which a finished cycle leaves at zero.
+int clear_after_abort(swe_world* w) {
+  if (!w->scratch_dirty) return SWE_OK;
+  w->scratch_dirty = false;
+  const size_t stride = ((size_t)w->n + 63) & ~(size_t)63;
+  SWE_CK(cudaMemsetAsync(w->pb.dq, 0, sizeof(int32_t) * 4 * stride, w->stream));
   return SWE_OK;
 }
 
@@ -418,10 +436,17 @@ int swe_world_erode(swe_world* w, int cycles, int particles, swe_mode mode) {
   }
   const int lanes = swe::par_lanes(w->p.lanes, w->nx, w->nz, particles);
   if (int rc = ensure_parallel(w, lanes)) return rc;
+  if (int rc = clear_after_abort(w)) return rc;
   if (int rc = ensure_fixed(w)) return rc;
   SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, w->stream));
   for (int k = 0; k < cycles; k++)
     if (int rc = enqueue_parallel_cycle(w, particles, lanes)) return rc;
+  return SWE_OK;
+}
+
+int swe_world_set_wait_limit(swe_world* w, uint64_t ns) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  w->wait_ns = ns;
   return SWE_OK;
 }
 
@@ -469,6 +494,7 @@ int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* 
     if (cycles == 0) continue;
     const int lanes = swe::par_lanes(w->p.lanes, w->nx, w->nz, particles);
     if (int rc = ensure_parallel(w, lanes)) return rc;
+    if (int rc = clear_after_abort(w)) return rc;
     if (int rc = ensure_fixed(w)) return rc;
     SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, w->stream));
     if (swe::batch_fits(lanes, w->nx, w->nz)) {
@@ -503,6 +529,275 @@ int swe_batch_erode(swe_world* const* worlds, int count, int cycles, const int* 
   }
   SWE_CK(swe::launch_par_batch(fit.data(), (int)fit.size(), cycles, s));
   return SWE_OK;
+}
+
+}  // extern "C"
+
+struct swe_batch {
+  std::vector<swe_world*> worlds;
+  std::vector<int> particles;
+  std::vector<int> lanes;
+  swe::BatchShape shape{16, 256};
+  int clusters = 0;       // clusters launched for `shape`
+  void* d_mem = nullptr;  // queue counter (first 256 bytes), then the world entries
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  double tuned_ms = 0.0, default_ms = 0.0;
+};
+
+namespace {
+
+std::mutex g_tune_mutex;
+std::map<std::string, swe::BatchShape> g_tuned;  // batch signature -> fastest shape
+
+std::string batch_signature(const swe_batch& b) {
+  std::vector<std::string> parts;
+  for (size_t i = 0; i < b.worlds.size(); i++) {
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "%dx%d:%d:%d", b.worlds[i]->nx, b.worlds[i]->nz, b.particles[i], b.lanes[i]);
+    parts.emplace_back(buf);
+  }
+  std::sort(parts.begin(), parts.end());
+  std::string key;
+  for (auto& p : parts) key += p + ";";
+  return key;
+}
+
+std::vector<swe::BatchWorld> batch_worlds(const std::vector<swe_world*>& ws, const std::vector<int>& particles,
+                                          const std::vector<int>& lanes) {
+  std::vector<swe::BatchWorld> out(ws.size());
+  for (size_t i = 0; i < ws.size(); i++) {
+    swe::BatchWorld& b = out[i];
+    b.B = ws[i]->pb;
+    b.F = ws[i]->F;
+    b.c = ws[i]->consts();
+    b.seed = ws[i]->seed;
+    b.cnt = ws[i]->cnt;
+    b.gb = ws[i]->gbar;
+    b.particles = particles[i];
+    b.lanes = lanes[i];
+  }
+  return out;
+}
+
+// Per world before a run: the tallies the world API resets per call, and the
+// scratch an aborted cycle left behind.
+int batch_prelude(swe_batch* b) {
+  for (swe_world* w : b->worlds) {
+    SWE_CK(cudaMemsetAsync(w->cnt, 0, 3 * sizeof(unsigned long long), b->stream));
+    SWE_CK(cudaMemsetAsync(&w->cnt->fly_ns, 0, 17 * sizeof(unsigned long long) + 8, b->stream));
+  }
+  return SWE_OK;
+}
+
+// Times one cycle of shape `sh` on the scratch worlds `rep` (ms; < 0: the
+// shape cannot run this batch).
+double time_shape(swe_batch* b, const std::vector<swe_world*>& rep, const swe::BatchShape& sh, void* d_mem) {
+  const int clusters = swe::batch_clusters(sh, (int)rep.size());
+  if (clusters < 1) return -1.0;
+  const std::vector<swe::BatchWorld> bw = batch_worlds(rep, b->particles, b->lanes);
+  void* d_items = static_cast<char*>(d_mem) + 256;
+  if (swe::upload_batch_items(bw.data(), (int)bw.size(), sh, d_items, b->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.0;
+  }
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return -1.0;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return -1.0;
+  }
+  double ms = -1.0;
+  cudaError_t e = cudaEventRecord(e0, b->stream);
+  if (e == cudaSuccess)
+    e = swe::launch_batch_items(d_items, static_cast<unsigned*>(d_mem), (int)bw.size(), 1, sh, clusters, b->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float f = 0.0f;
+  if (e == cudaSuccess && cudaEventElapsedTime(&f, e0, e1) == cudaSuccess) ms = f;
+  if (e != cudaSuccess) cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
+// The autotuner: one cycle of every feasible shape on scratch copies of the
+// worlds (same sizes, parameters, seeds and heights), fastest wins.
+int tune_batch(swe_batch* b) {
+  const std::string key = batch_signature(*b);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      b->shape = it->second;
+      return SWE_OK;
+    }
+  }
+  std::vector<swe_world*> rep;
+  auto cleanup = [&]() {
+    for (swe_world* r : rep) swe_world_destroy(r);
+  };
+  for (size_t i = 0; i < b->worlds.size(); i++) {
+    swe_world* w = b->worlds[i];
+    swe_world* r = nullptr;
+    int rc = swe_world_create(w->nx, w->nz, &w->p, w->seed, &r);
+    if (rc != SWE_OK) {
+      cleanup();
+      return rc;
+    }
+    rep.push_back(r);
+    // everything of the tuning runs on the batch's stream
+    cudaStreamDestroy(r->stream);
+    r->stream = b->stream;
+    r->own_stream = false;
+    if (cudaMemcpyAsync(r->F.f[0], w->F.f[0], sizeof(float) * (size_t)w->n, cudaMemcpyDeviceToDevice, b->stream) !=
+        cudaSuccess) {
+      cleanup();
+      return fail(SWE_ERR_CUDA, "copying a height map for the autotuner failed");
+    }
+    if ((rc = ensure_parallel(r, b->lanes[i])) != SWE_OK || (rc = ensure_fixed(r)) != SWE_OK) {
+      cleanup();
+      return rc;
+    }
+  }
+  static const swe::BatchShape kShapes[] = {{16, 256}, {16, 128}, {8, 256}, {8, 128}, {4, 256}, {4, 128}};
+  double best = -1.0;
+  swe::BatchShape best_shape{16, 256};
+  time_shape(b, rep, kShapes[0], b->d_mem);  // warm-up: first launch of the kernel
+  for (const swe::BatchShape& sh : kShapes) {
+    const double ms = time_shape(b, rep, sh, b->d_mem);
+    if (sh.ctas == 16 && sh.threads == 256) b->default_ms = ms > 0 ? ms : 0.0;
+    if (ms > 0 && (best < 0 || ms < best)) {
+      best = ms;
+      best_shape = sh;
+    }
+  }
+  cleanup();
+  rep.clear();
+  if (best < 0) return fail(SWE_ERR_CUDA, "no launch shape of the batch kernel can run this ensemble");
+  b->shape = best_shape;
+  b->tuned_ms = best;
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tuned[key] = best_shape;
+  return SWE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swe_batch_create(swe_world* const* worlds, int count, const int* particles_per_cycle, int tune, swe_batch** out) {
+  if (!out) return fail(SWE_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (count < 1 || !worlds || !particles_per_cycle) return fail(SWE_ERR_INVALID, "a batch needs count >= 1 worlds");
+  for (int i = 0; i < count; i++) {
+    if (!worlds[i]) return fail(SWE_ERR_INVALID, "a world is NULL");
+    if (particles_per_cycle[i] < 0) return fail(SWE_ERR_INVALID, "particles_per_cycle must be >= 0");
+    if (worlds[i]->device != worlds[0]->device) return fail(SWE_ERR_INVALID, "worlds on different devices");
+  }
+  {
+    std::vector<swe_world*> sorted(worlds, worlds + count);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(SWE_ERR_INVALID, "a world appears twice in the batch");
+  }
+  if (int rc = use_device(worlds[0])) return rc;
+  swe_batch* b = new swe_batch();
+  b->device = worlds[0]->device;
+  b->stream = worlds[0]->stream;
+  auto bail = [&](int rc) {
+    std::string msg = g_error;
+    swe_batch_destroy(b);
+    g_error = msg;
+    return rc;
+  };
+  for (int i = 0; i < count; i++) {
+    swe_world* w = worlds[i];
+    const int lanes = swe::par_lanes(w->p.lanes, w->nx, w->nz, particles_per_cycle[i]);
+    if (!swe::batch_fits(lanes, w->nx, w->nz))
+      return bail(fail(SWE_ERR_INVALID, "a world has more particles in flight than one cluster holds (16,384)"));
+    // everything queued on the worlds' own streams comes first
+    if (cudaStreamSynchronize(w->stream) != cudaSuccess) return bail(fail(SWE_ERR_CUDA, "a world's stream failed"));
+    if (int rc = ensure_parallel(w, lanes)) return bail(rc);
+    if (int rc = clear_after_abort(w)) return bail(rc);
+    if (int rc = ensure_fixed(w)) return bail(rc);
+    if (cudaStreamSynchronize(w->stream) != cudaSuccess) return bail(fail(SWE_ERR_CUDA, "a world's stream failed"));
+    b->worlds.push_back(w);
+    b->particles.push_back(particles_per_cycle[i]);
+    b->lanes.push_back(lanes);
+  }
+  if (cudaMalloc(&b->d_mem, 256 + swe::batch_item_bytes() * (size_t)count) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(fail(SWE_ERR_NO_MEMORY, "cannot allocate the batch's device entries"));
+  }
+  if (tune)
+    if (int rc = tune_batch(b)) return bail(rc);
+  b->clusters = swe::batch_clusters(b->shape, count);
+  if (b->clusters < 1) return bail(fail(SWE_ERR_CUDA, "the batch kernel cannot launch on this device"));
+  const std::vector<swe::BatchWorld> bw = batch_worlds(b->worlds, b->particles, b->lanes);
+  const cudaError_t e = swe::upload_batch_items(bw.data(), count, b->shape, static_cast<char*>(b->d_mem) + 256,
+                                                b->stream);
+  if (e != cudaSuccess) return bail(fail(SWE_ERR_CUDA, std::string("batch entries: ") + cudaGetErrorString(e)));
+  *out = b;
+  return SWE_OK;
+}
+
+int swe_batch_run(swe_batch* b, int cycles) {
+  if (!b) return fail(SWE_ERR_INVALID, "NULL batch");
+  if (cycles < 0) return fail(SWE_ERR_INVALID, "cycles must be >= 0");
+  SWE_CK(cudaSetDevice(b->device));
+  if (int rc = batch_prelude(b)) return rc;
+  if (cycles == 0) return SWE_OK;
+  for (swe_world* w : b->worlds) {
+    if (w->scratch_dirty) {
+      w->scratch_dirty = false;
+      const size_t stride = ((size_t)w->n + 63) & ~(size_t)63;
+      SWE_CK(cudaMemsetAsync(w->pb.dq, 0, sizeof(int32_t) * 4 * stride, b->stream));
+    }
+    if (!w->hq_valid) {
+      swe::launch_height_to_fixed(w->F.f[0], w->pb.hq, w->consts(), w->cnt, b->stream);
+      SWE_CK(cudaGetLastError());
+      w->hq_valid = true;
+    }
+  }
+  SWE_CK(swe::launch_batch_items(static_cast<char*>(b->d_mem) + 256, static_cast<unsigned*>(b->d_mem),
+                                 (int)b->worlds.size(), cycles, b->shape, b->clusters, b->stream));
+  return SWE_OK;
+}
+
+int swe_batch_shape(swe_batch* b, int* ctas_per_cluster, int* threads_per_cta, double* tuned_ms, double* default_ms) {
+  if (!b) return fail(SWE_ERR_INVALID, "NULL batch");
+  if (ctas_per_cluster) *ctas_per_cluster = b->shape.ctas;
+  if (threads_per_cta) *threads_per_cta = b->shape.threads;
+  if (tuned_ms) *tuned_ms = b->tuned_ms;
+  if (default_ms) *default_ms = b->default_ms;
+  return SWE_OK;
+}
+
+int swe_batch_set_shape(swe_batch* b, int ctas_per_cluster, int threads_per_cta) {
+  if (!b) return fail(SWE_ERR_INVALID, "NULL batch");
+  const swe::BatchShape sh{ctas_per_cluster, threads_per_cta};
+  if (!swe::batch_shape_ok(sh))
+    return fail(SWE_ERR_INVALID, "ctas_per_cluster must be 4, 8 or 16 and threads_per_cta a multiple of 32 up to 256");
+  SWE_CK(cudaSetDevice(b->device));
+  const int clusters = swe::batch_clusters(sh, (int)b->worlds.size());
+  if (clusters < 1) return fail(SWE_ERR_INVALID, "this shape cannot launch");
+  const std::vector<swe::BatchWorld> bw = batch_worlds(b->worlds, b->particles, b->lanes);
+  const cudaError_t e = swe::upload_batch_items(bw.data(), (int)bw.size(), sh, static_cast<char*>(b->d_mem) + 256,
+                                                b->stream);
+  if (e == cudaErrorInvalidValue) return fail(SWE_ERR_INVALID, "a world's lanes do not fit one cluster of this shape");
+  SWE_CK(e);
+  b->shape = sh;
+  b->clusters = clusters;
+  return SWE_OK;
+}
+
+void swe_batch_destroy(swe_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  cudaFree(b->d_mem);
+  delete b;
 }
 
 int swe_batch_erode_ordered(swe_world* const* worlds, int count, int cycles, const int* particles_per_cycle) {
@@ -572,6 +867,7 @@ int swe_world_status(swe_world* w, uint32_t* status) {
   SWE_CK(cudaStreamSynchronize(w->stream));
   unsigned int st = 0;
   SWE_CK(cudaMemcpy(&st, &w->cnt->status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st & SWE_STATUS_TIMEOUT) w->scratch_dirty = true;
   if (status) *status = st;
   return SWE_OK;
 }
@@ -583,9 +879,11 @@ int swe_world_sync(swe_world* w) {
   if (st) {
     SWE_CK(cudaMemset(&w->cnt->status, 0, sizeof(unsigned int)));
     char buf[160];
-    std::snprintf(buf, sizeof buf, "device status 0x%x:%s%s%s", st, (st & SWE_STATUS_NONFINITE) ? " non-finite particle" : "",
+    std::snprintf(buf, sizeof buf, "device status 0x%x:%s%s%s%s", st,
+                  (st & SWE_STATUS_NONFINITE) ? " non-finite particle" : "",
                   (st & SWE_STATUS_RANGE) ? " fixed-point height out of range" : "",
-                  (st & SWE_STATUS_TAPE) ? " rand tape exhausted" : "");
+                  (st & SWE_STATUS_TAPE) ? " rand tape exhausted" : "",
+                  (st & SWE_STATUS_TIMEOUT) ? " a wait ran past its deadline (cycle aborted)" : "");
     return fail(SWE_ERR_DEVICE, buf);
   }
   return SWE_OK;

@@ -75,6 +75,13 @@ int cycle_grid(int device);
 // One parallel erode cycle as one cooperative kernel.
 cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
                              Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s);
+// Whether `lanes` particles in flight on an n-cell map take the bounded-lanes
+// kernel (one 16-CTA cluster, or one CTA per SM), whose particle state lives
+// in shared memory; otherwise launch_par_cycle needs B.state to hold them.
+bool lanes_form_fits(int lanes, long n);
+// Sets the cycle counter (which keys the parallel mode's random numbers) on
+// the device, in stream order.
+void launch_set_cycle(Counters* cnt, uint64_t cycle, cudaStream_t s);
 // Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/64),
 // < 0 -> all particles of the cycle; never more than the cycle's particles.
 int par_lanes(int lanes, int nx, int nz, int particles);
@@ -110,12 +117,38 @@ struct BatchWorld {
   int particles;  // per cycle
   int lanes;      // particles in flight (par_lanes)
 };
-// Whether a world with `lanes` in flight fits one cluster of the batch kernel.
+// Whether a world with `lanes` in flight fits one 16-CTA cluster of the batch kernel.
 bool batch_fits(int lanes, int nx, int nz);
 // `cycles` parallel erode cycles of every world in one persistent launch of
 // 16-CTA clusters on stream s (the worlds' height maps already in fixed
 // point). Returns after the launch has completed.
 cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s);
+// Launch shape of the batch kernel: CTAs per cluster (4, 8 or 16; one world
+// per cluster at a time) and threads per CTA (a multiple of 32 up to 256).
+// It changes no result: a world's lanes are spread over its cluster's
+// threads, and only the set of particles in flight matters.
+struct BatchShape {
+  int ctas;
+  int threads;
+};
+bool batch_shape_ok(const BatchShape& sh);
+// Bytes of one world's entry in the device array of a prepared batch.
+size_t batch_item_bytes();
+// Writes the entries of `count` worlds for shape `sh` to d_items (device,
+// count * batch_item_bytes()); returns after the copy. cudaErrorInvalidValue
+// if a world's lanes do not fit one cluster of that shape.
+cudaError_t upload_batch_items(const BatchWorld* worlds, int count, const BatchShape& sh, void* d_items,
+                               cudaStream_t s);
+// Clusters of shape `sh` to launch for a batch of `count` worlds: those that
+// run at once, at most `count` (0: the shape cannot launch). Also sets the
+// kernel's launch attributes, so call it before launch_batch_items.
+int batch_clusters(const BatchShape& sh, int count);
+// `cycles` cycles of a prepared batch on `clusters` clusters: resets the
+// queue counter (d_queue, device) and launches the persistent kernel on s.
+// Only a memset and a kernel launch are enqueued, so it can be captured into
+// a CUDA graph.
+cudaError_t launch_batch_items(const void* d_items, unsigned* d_queue, int count, int cycles, const BatchShape& sh,
+                               int clusters, cudaStream_t s);
 
 // ---- learned surrogate building blocks (swe_surrogate.cu): bf16 NHWC ----
 cudaError_t nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int N, int H, int W, int cin,

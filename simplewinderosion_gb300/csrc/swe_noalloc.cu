@@ -5,11 +5,12 @@
 // app erodes once per rendered frame, SimpleWindErosion.cpp:212-231), or code
 // running while another framework's allocator owns the device memory. They
 // still own the nine cell fields (inputs and outputs), but not the scratch
-// the parallel kernel needs: fixed-point maps, track accumulators, particle
-// state, counters and the grid barrier. swe_erode_parallel_noalloc keeps that
-// scratch in one file-scope device array of fixed size, so it allocates
-// nothing; every GPU that loads the library holds the array until the
-// process exits.
+// the parallel kernel needs: fixed-point maps, track accumulators, counters
+// and the grid barrier (particle state stays in shared memory: the call
+// takes only the bounded-lanes kernel forms). swe_erode_parallel_noalloc
+// keeps that scratch in one file-scope device array of fixed size, so it
+// allocates nothing; every GPU that loads the library holds the array until
+// the process exits.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -32,9 +33,7 @@ constexpr size_t kBitWords = ((kMaxCells + 128) / 32 + 2 + 63) & ~(size_t)63;  /
 constexpr size_t kMapsBytes = (7 * kMaxCells + 3 * kBitWords) * sizeof(int32_t);
 constexpr size_t kTracksBytes = 4 * kMaxCells * sizeof(long long);   // track accumulators
 constexpr size_t kWordsBytes = (kMaxCells + 32) * sizeof(unsigned long long);  // height words + padding
-constexpr size_t kParticleBytes = 2 * 9 * kMaxParticles * sizeof(int32_t);  // two state buffers
-constexpr size_t kScratchBytes =
-    kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes + kWordsBytes + kParticleBytes;
+constexpr size_t kScratchBytes = kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes + kWordsBytes;
 
 // The scratch. In host code this name is only a stand-in for the device
 // object: its device address comes from cudaGetSymbolAddress, per device.
@@ -109,7 +108,10 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   const long n = (long)nx * nz;
   const size_t stride = ((size_t)n + 63) & ~(size_t)63;
   const int lanes = swe::par_lanes(p->lanes, nx, nz, particles_per_cycle);
-  const int cap = lanes > 0 ? lanes : 1;
+  // Particles in flight live in the bounded-lanes kernel's shared memory;
+  // the all-at-once kernel would need particle buffers this call lacks.
+  if (!swe::lanes_form_fits(lanes, n))
+    return fail(SWE_ERR_INVALID, "more particles in flight than the bounded-lanes kernel holds on this GPU");
   unsigned char* base = ds->base;
   swe::Counters* cnt = reinterpret_cast<swe::Counters*>(base);
   swe::GridBarrier* gb = reinterpret_cast<swe::GridBarrier*>(base + kCountersBytes);
@@ -117,8 +119,6 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   long long* tracks = reinterpret_cast<long long*>(base + kCountersBytes + kBarrierBytes + kMapsBytes);
   unsigned long long* words =
       reinterpret_cast<unsigned long long*>(base + kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes);
-  int32_t* pstate = reinterpret_cast<int32_t*>(base + kCountersBytes + kBarrierBytes + kMapsBytes + kTracksBytes +
-                                               kWordsBytes);
 
   swe::ParallelBuffers B{};
   B.hq = maps;
@@ -132,20 +132,7 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   B.vbits_words = (long)((n + 128) / 32 + 2);
   B.hw = words + 1;  // one padding word before (and after) the map
   for (int k = 0; k < 4; k++) B.tq[k] = tracks + (size_t)k * n;
-  for (int b = 0; b < 2; b++) {
-    int32_t* q = pstate + (size_t)b * 9 * cap;
-    swe::ParticleSoA& S = B.state[b];
-    S.id = q;
-    S.age = q + 1 * (size_t)cap;
-    S.px = reinterpret_cast<float*>(q + 2 * (size_t)cap);
-    S.py = reinterpret_cast<float*>(q + 3 * (size_t)cap);
-    S.pz = reinterpret_cast<float*>(q + 4 * (size_t)cap);
-    S.vx = reinterpret_cast<float*>(q + 5 * (size_t)cap);
-    S.vy = reinterpret_cast<float*>(q + 6 * (size_t)cap);
-    S.vz = reinterpret_cast<float*>(q + 7 * (size_t)cap);
-    S.sed_q = q + 8 * (size_t)cap;
-  }
-  B.capacity = cap;
+  B.capacity = 0;  // no particle buffers (B.state stays null)
 
   swe::Fields F;
   for (int k = 0; k < 9; k++) F.f[k] = fields[k];
@@ -169,9 +156,10 @@ extern "C" int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, 
   c.inv_scale = 1.0f / c.scale;
 
   // The array keeps the last call's contents: reset everything a cycle
-  // expects at zero, then set the random-number cycle counter.
+  // expects at zero, then set the random-number cycle counter (by a kernel
+  // argument, so nothing is read from host memory later).
   SWE_NA_CK(cudaMemsetAsync(cnt, 0, sizeof(swe::Counters), s));
-  SWE_NA_CK(cudaMemcpyAsync(&cnt->cycle, &first_cycle, sizeof(first_cycle), cudaMemcpyHostToDevice, s));
+  swe::launch_set_cycle(cnt, first_cycle, s);
   SWE_NA_CK(cudaMemsetAsync(B.dq, 0, 2 * stride * sizeof(int32_t), s));
   SWE_NA_CK(cudaMemsetAsync(B.dq2, 0, 2 * stride * sizeof(int32_t), s));
   swe::launch_height_to_fixed(F.f[0], B.hq, c, cnt, s);

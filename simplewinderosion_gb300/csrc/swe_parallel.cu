@@ -35,8 +35,9 @@
 // integers in units of 2^-32; particle sediment is fixed point like heights.
 //
 // The grid barrier spins with an explicit deadline: a block that waits longer
-// than 2 s sets SWE_STATUS_TIMEOUT and an abort flag, and every block then
-// leaves the kernel at its next barrier, so the kernel always ends.
+// than the wait limit (Consts::wait_ns, 2 s by default) sets
+// SWE_STATUS_TIMEOUT and an abort flag, and every block then leaves the
+// kernel at its next barrier, so the kernel always ends.
 #include <algorithm>
 #include <vector>
 
@@ -51,7 +52,11 @@ constexpr float kInvTwo32 = 2.3283064365386963e-10f;
 constexpr float kSqrt2 = 1.41421354f;  // sqrtf(2.0f), correctly rounded
 constexpr int kCycleThreads = 256;
 constexpr int kCycleBlocksPerSm = 4;  // 64 registers per thread, no spills
-constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // the default wait deadline
+
+__host__ __device__ __forceinline__ unsigned long long wait_limit(const Consts& c) {
+  return c.wait_ns ? c.wait_ns : kBarrierLimitNs;
+}
 
 __device__ __forceinline__ float fx2f(int32_t q, float inv) { return __int2float_rn(q) * inv; }
 __device__ __forceinline__ int32_t wrap_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
@@ -95,10 +100,10 @@ __device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
 // value its own arrival returned (release/acquire atomics, no separate
 // fences, no generation word to read first or to publish last). Thread 0
 // arrives for its block; the block barriers before and after carry the rest
-// of the block's threads. Every wait has a 2 s deadline, after which the
+// of the block's threads. Every wait has a deadline (`limit`), after which the
 // block sets SWE_STATUS_TIMEOUT and the abort flag; returns false if the
 // kernel must stop.
-__device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
+__device__ bool grid_sync(GridBarrier* gb, unsigned int* status, unsigned long long limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -111,7 +116,7 @@ __device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
         ok = 0;
         break;
       }
-      if (global_ns() - t0 > kBarrierLimitNs) {
+      if (global_ns() - t0 > limit) {
         atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
         atomicExch(&gb->abort, 1u);
         ok = 0;
@@ -135,8 +140,8 @@ __device__ bool grid_sync(GridBarrier* gb, unsigned int* status) {
 // in for a block order), *total the sum over all blocks, read after the flip.
 // Block 0 clears sums[phase + 1 mod 3] before it arrives: that counter's last
 // total was read two barriers ago, and its next counts come after this one.
-__device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned phase, unsigned mine,
-                              unsigned* below, unsigned* total) {
+__device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned long long limit, unsigned phase,
+                              unsigned mine, unsigned* below, unsigned* total) {
   __shared__ int s_ok;
   __shared__ unsigned s_below, s_total;
   __syncthreads();
@@ -153,7 +158,7 @@ __device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned ph
         ok = 0;
         break;
       }
-      if (global_ns() - t0 > kBarrierLimitNs) {
+      if (global_ns() - t0 > limit) {
         atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
         atomicExch(&gb->abort, 1u);
         ok = 0;
@@ -799,7 +804,7 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
   };
 
   spawn_phase(A, c_lo, c_hi);
-  if (!grid_sync(A.gb, &cnt->status)) return;
+  if (!grid_sync(A.gb, &cnt->status, wait_limit(A.c))) return;
   lap(0);
 
   CascadeStats cst;
@@ -811,7 +816,7 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
     const int count = ld_volatile(&cnt->live[in]) + ld_volatile(&cnt->refill[in]);
     if (count == 0) break;
     fly_phase(A, in, count, c_lo, c_hi);
-    if (!grid_sync(A.gb, &cnt->status)) return;
+    if (!grid_sync(A.gb, &cnt->status, wait_limit(A.c))) return;
     lap(1);
     // Survivors and the particles that take the freed lanes; every block
     // reads the same counters here and computes the same refill.
@@ -829,13 +834,13 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
       // Only survivors wrote D and C: nothing to cascade.
       if (refill == 0) break;
       refill_lanes(A, outp, survivors, nid, refill, c_lo, c_hi);
-      if (!grid_sync(A.gb, &cnt->status)) return;
+      if (!grid_sync(A.gb, &cnt->status, wait_limit(A.c))) return;
       continue;
     }
     for (int col = 0; col < 9; col++) {
       if (col == 0) refill_lanes(A, outp, survivors, nid, refill, c_lo, c_hi);
       colour_phase(A, col / 3, col % 3, nb, list, owed, wcount, cst);
-      if (!grid_sync(A.gb, &cnt->status)) return;
+      if (!grid_sync(A.gb, &cnt->status, wait_limit(A.c))) return;
       lap(3 + col);
     }
   }
@@ -913,7 +918,7 @@ __global__ void __launch_bounds__(kCycleThreads, kCycleBlocksPerSm) k_par_cycle(
 // in colour order, the polling loops are warp-uniform (a lane that is not
 // ready polls again on the next pass, so it never holds up a lane of its own
 // warp), and the CTAs are co-resident, so every wait ends. Each wait still
-// has a 2 s deadline: past it the thread sets SWE_STATUS_TIMEOUT and the
+// has a deadline (2 s unless the world sets another): past it the thread sets SWE_STATUS_TIMEOUT and the
 // abort flag, tagged with the barrier count, and every thread leaves the step
 // loop after the same barrier.
 // ---------------------------------------------------------------------------
@@ -931,6 +936,12 @@ __device__ __forceinline__ void cluster_barrier() {
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ unsigned cluster_ctas() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
   return r;
 }
 
@@ -1021,7 +1032,7 @@ struct BlockBits {
 template <bool kCluster>
 __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32_t* dyn) {
   __shared__ int s_free[2];            // free lanes of this CTA by step parity, read by the other CTAs
-  __shared__ int s_all[kClusterCtas];  // every CTA's free lanes, this step
+  __shared__ int s_all[kClusterCtas];  // every CTA's free lanes, this step (clusters of up to 16 CTAs)
   __shared__ int s_warp[32];
   __shared__ unsigned long long s_time[3];  // fly, cascades, last mark (CTA 0's thread 0)
   const int T = blockDim.x;
@@ -1053,7 +1064,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   Counters* cnt = A.cnt;
   const int nx = c.nx, nz = c.nz;
   const unsigned r = kCluster ? cluster_rank() : blockIdx.x;
-  const int nb = kCluster ? kClusterCtas : (int)gridDim.x;
+  const int nb = kCluster ? (int)cluster_ctas() : (int)gridDim.x;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
   const unsigned long long cyc = cnt->cycle;
   const uint32_t c_lo = (uint32_t)cyc, c_hi = (uint32_t)(cyc >> 32);
@@ -1247,7 +1258,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         if (ready != need && !gave_up) {
           const unsigned long long now = global_ns();
           if (t_wait == 0) t_wait = now;
-          if (now - t_wait > kBarrierLimitNs || ld_volatile(reinterpret_cast<const int*>(&A.gb->abort)) != 0) {
+          if (now - t_wait > wait_limit(c) || ld_volatile(reinterpret_cast<const int*>(&A.gb->abort)) != 0) {
             status |= 0x8u;  // SWE_STATUS_TIMEOUT
             atomicCAS(&A.gb->abort, 0u, ph + 1);
             gave_up = true;
@@ -1294,17 +1305,16 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       cluster_barrier();
       ph++;
       if (aborted_before(A.gb, ph)) break;
-      if (t < kClusterCtas) s_all[t] = ld_dsmem(&s_free[odd], (unsigned)t);
+      if (t < nb) s_all[t] = ld_dsmem(&s_free[odd], (unsigned)t);
       __syncthreads();
-#pragma unroll
-      for (int k = 0; k < kClusterCtas; k++) {
+      for (int k = 0; k < nb; k++) {
         const int v = s_all[k];
         total_free += v;
         base += k < (int)r ? v : 0;
       }
     } else {
       unsigned below = 0, tot = 0;
-      if (!grid_sync_sum(A.gb, &cnt->status, rot, (unsigned)btotal, &below, &tot)) break;
+      if (!grid_sync_sum(A.gb, &cnt->status, wait_limit(c), rot, (unsigned)btotal, &below, &tot)) break;
       ph++;
       total_free = (int)tot;
       base = (int)below;
@@ -1465,7 +1475,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
             // Not ready: a deadline, and the abort flag of another thread.
             const unsigned long long now = global_ns();
             if (t_wait == 0) t_wait = now;
-            if (now - t_wait > kBarrierLimitNs || ld_volatile(reinterpret_cast<const int*>(&A.gb->abort)) != 0) {
+            if (now - t_wait > wait_limit(c) || ld_volatile(reinterpret_cast<const int*>(&A.gb->abort)) != 0) {
               if (!gave_up) {
                 status |= 0x8u;  // SWE_STATUS_TIMEOUT
                 atomicCAS(&A.gb->abort, 0u, ph + 1);
@@ -1559,7 +1569,7 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1)
   __shared__ int s_slots;
   const unsigned r = cluster_rank();
   const int T = blockDim.x;
-  const long tid = (long)r * T + threadIdx.x, nthr = (long)kClusterCtas * T;
+  const long tid = (long)r * T + threadIdx.x, nthr = (long)cluster_ctas() * T;
   for (;;) {
     if (r == 0 && threadIdx.x == 0) s_item = (int)atomicAdd(queue, 1u);
     cluster_barrier();
@@ -1747,9 +1757,26 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
       return cudaGetLastError();
     }
   }
+  // All particles at once: the particle state lives in B.state.
+  if (B.capacity < lanes || !B.state[0].id) return cudaErrorInvalidValue;
   void* args[] = {&A};
   return cudaLaunchCooperativeKernel((const void*)k_par_cycle, dim3(grid), dim3(kCycleThreads), args, 0, s);
 }
+
+bool lanes_form_fits(int lanes, long n) {
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms > 1024) sms = 1024;
+  int threads = 0, slots = 0;
+  const bool cluster = lanes <= kClusterMaxLanes;
+  return n <= (1l << 30) && lanes_shape(lanes, cluster ? kClusterCtas : sms,
+                                        cluster ? kClusterMaxThreads : kLanesGridMaxThreads, &threads, &slots);
+}
+
+__global__ void k_set_cycle(Counters* cnt, unsigned long long cycle) { cnt->cycle = cycle; }
+
+void launch_set_cycle(Counters* cnt, uint64_t cycle, cudaStream_t s) { k_set_cycle<<<1, 1, 0, s>>>(cnt, cycle); }
 
 bool batch_fits(int lanes, int nx, int nz) {
   int threads = 0, slots = 0;
@@ -1757,8 +1784,16 @@ bool batch_fits(int lanes, int nx, int nz) {
          lanes_shape(lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots);
 }
 
-cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s) {
-  if (count <= 0 || cycles <= 0) return cudaSuccess;
+bool batch_shape_ok(const BatchShape& sh) {
+  return (sh.ctas == 4 || sh.ctas == 8 || sh.ctas == 16) && sh.threads >= 32 && sh.threads <= kClusterMaxThreads &&
+         sh.threads % 32 == 0;
+}
+
+size_t batch_item_bytes() { return sizeof(BatchItem); }
+
+cudaError_t upload_batch_items(const BatchWorld* worlds, int count, const BatchShape& sh, void* d_items,
+                               cudaStream_t s) {
+  if (!batch_shape_ok(sh)) return cudaErrorInvalidValue;
   // Largest worlds first (cells x particles), so that the last clusters to
   // finish are not the ones that started the longest worlds last.
   std::vector<int> order((size_t)count);
@@ -1782,44 +1817,80 @@ cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cu
     A.particles = w.particles;
     A.lanes = w.lanes;
     int threads = 0, slots = 0;
-    if (!lanes_shape(w.lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots)) return cudaErrorInvalidValue;
+    if ((long)w.c.nx * w.c.nz > (1l << 30) || !lanes_shape(w.lanes, sh.ctas, sh.threads, &threads, &slots))
+      return cudaErrorInvalidValue;
     items[i].slots = slots;
     items[i].pad = 0;
   }
+  cudaError_t e = cudaMemcpyAsync(d_items, items.data(), sizeof(BatchItem) * (size_t)count, cudaMemcpyHostToDevice, s);
+  // the host array must outlive the copy
+  const cudaError_t es = cudaStreamSynchronize(s);
+  return e != cudaSuccess ? e : es;
+}
+
+namespace {
+
+void batch_launch_config(const BatchShape& sh, int clusters, cudaStream_t s, cudaLaunchConfig_t* cfg,
+                         cudaLaunchAttribute* attr) {
+  *cfg = cudaLaunchConfig_t{};
+  cfg->gridDim = dim3(sh.ctas * clusters);
+  cfg->blockDim = dim3(sh.threads);
+  cfg->dynamicSmemBytes = lanes_smem(sh.threads, kClusterMaxSlots);
+  cfg->stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = sh.ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg->attrs = attr;
+  cfg->numAttrs = 1;
+}
+
+}  // namespace
+
+int batch_clusters(const BatchShape& sh, int count) {
+  if (!batch_shape_ok(sh) || count < 1) return 0;
+  // the largest shared-memory size any shape asks for
   const size_t smem = lanes_smem(kClusterMaxThreads, kClusterMaxSlots);
   cudaError_t e = cudaFuncSetAttribute(k_par_batch, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_par_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kClusterCtas);
-  cfg.blockDim = dim3(kClusterMaxThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
+  cudaLaunchConfig_t cfg;
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kClusterCtas;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  batch_launch_config(sh, 1, nullptr, &cfg, attr);
   int clusters = 0;
-  e = cudaOccupancyMaxActiveClusters(&clusters, k_par_batch, &cfg);
-  if (e != cudaSuccess) return e;
-  if (clusters < 1) return cudaErrorCooperativeLaunchTooLarge;
-  if (clusters > count) clusters = count;
-  cfg.gridDim = dim3(kClusterCtas * clusters);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&clusters, k_par_batch, &cfg);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return clusters < count ? clusters : count;
+}
+
+cudaError_t launch_batch_items(const void* d_items, unsigned* d_queue, int count, int cycles, const BatchShape& sh,
+                               int clusters, cudaStream_t s) {
+  if (count <= 0 || cycles <= 0) return cudaSuccess;
+  if (!batch_shape_ok(sh) || clusters < 1) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute attr[1];
+  batch_launch_config(sh, clusters, s, &cfg, attr);
+  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned), s);
+  if (e == cudaSuccess)
+    e = cudaLaunchKernelEx(&cfg, k_par_batch, static_cast<const BatchItem*>(d_items), count, cycles, d_queue);
+  return e;
+}
+
+cudaError_t launch_par_batch(const BatchWorld* worlds, int count, int cycles, cudaStream_t s) {
+  if (count <= 0 || cycles <= 0) return cudaSuccess;
+  const BatchShape sh{kClusterCtas, kClusterMaxThreads};
   // the items and the queue counter, freed in stream order after the launch
   const size_t bytes = sizeof(BatchItem) * (size_t)count + 256;
   void* d = nullptr;
-  e = cudaMallocAsync(&d, bytes, s);
+  cudaError_t e = cudaMallocAsync(&d, bytes, s);
   if (e != cudaSuccess) return e;
-  BatchItem* d_items = reinterpret_cast<BatchItem*>(static_cast<char*>(d) + 256);
+  void* d_items = static_cast<char*>(d) + 256;
   unsigned* d_queue = static_cast<unsigned*>(d);
-  e = cudaMemsetAsync(d_queue, 0, 256, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_items, items.data(), sizeof(BatchItem) * (size_t)count, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, k_par_batch, (const BatchItem*)d_items, count, cycles, d_queue);
-  // the host array must outlive the copy
+  const int clusters = batch_clusters(sh, count);
+  e = clusters < 1 ? cudaErrorCooperativeLaunchTooLarge : upload_batch_items(worlds, count, sh, d_items, s);
+  if (e == cudaSuccess) e = launch_batch_items(d_items, d_queue, count, cycles, sh, clusters, s);
   const cudaError_t es = cudaStreamSynchronize(s);
   cudaFreeAsync(d, s);
   return e != cudaSuccess ? e : es;

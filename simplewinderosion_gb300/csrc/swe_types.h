@@ -19,6 +19,9 @@ struct Consts {
   const uint32_t* expf_x;
   const int8_t* expf_d;
   int expf_n;
+  // Parallel mode: how long one wait (a grid barrier or a cell tag) may
+  // spin before the cycle is aborted with SWE_STATUS_TIMEOUT; 0 = 2 s.
+  unsigned long long wait_ns;
 };
 
 // State of the C library rand() replica: the last 34 elements of the

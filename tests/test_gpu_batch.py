@@ -61,3 +61,62 @@ def test_batch_rejects_a_world_twice():
         swe.batch_erode([w, w], 1, 100)
     assert e.value.code == -1
     w.close()
+
+
+# the worlds of ENSEMBLE that fit a 4-CTA cluster of 128 threads (at most 2,048 in flight)
+SMALL = ENSEMBLE[:5]
+
+
+@pytest.mark.parametrize("ctas,threads", [(16, 256), (8, 128), (4, 256), (4, 128)])
+def test_prepared_batch_any_shape_equals_worlds_alone(ctas, threads):
+    cycles = 2
+    batch = [_world(nx, nz, wind, fb, lanes, sd) for nx, nz, _, wind, fb, lanes, sd in SMALL]
+    alone = [_world(nx, nz, wind, fb, lanes, sd) for nx, nz, _, wind, fb, lanes, sd in SMALL]
+    particles = [e[2] for e in SMALL]
+    b = swe.Batch(batch, particles)
+    b.set_shape(ctas, threads)
+    assert b.shape()["ctas_per_cluster"] == ctas and b.shape()["threads_per_cta"] == threads
+    b.run(cycles)
+    for w, p in zip(alone, particles):
+        w.erode(p, cycles, mode=swe.Mode.PARALLEL)
+    for k, (a, c) in enumerate(zip(batch, alone)):
+        a.sync()
+        for f in swe.FIELDS:
+            assert np.array_equal(bits(a.download(f)), bits(c.download(f))), (ctas, threads, k, f)
+        assert a.mass_ledger() == c.mass_ledger(), k
+    b.close()
+    for w in batch + alone:
+        w.close()
+
+
+def test_autotuned_batch_equals_worlds_alone():
+    batch = [_world(nx, nz, wind, fb, lanes, sd) for nx, nz, _, wind, fb, lanes, sd in ENSEMBLE[:6]]
+    alone = [_world(nx, nz, wind, fb, lanes, sd) for nx, nz, _, wind, fb, lanes, sd in ENSEMBLE[:6]]
+    particles = [e[2] for e in ENSEMBLE[:6]]
+    b = swe.Batch(batch, particles, tune=True)
+    shape = b.shape()
+    assert shape["tuned_ms"] > 0 and shape["default_ms"] > 0
+    assert shape["tuned_ms"] <= shape["default_ms"]
+    b.run(1)
+    for w, p in zip(alone, particles):
+        w.erode(p, 1, mode=swe.Mode.PARALLEL)
+    for k, (a, c) in enumerate(zip(batch, alone)):
+        a.sync()
+        for f in swe.FIELDS:
+            assert np.array_equal(bits(a.download(f)), bits(c.download(f))), (shape, k, f)
+    # the same signature again: the cached shape, no measurement
+    b2 = swe.Batch(batch, particles, tune=True)
+    assert b2.shape()["ctas_per_cluster"] == shape["ctas_per_cluster"]
+    assert b2.shape()["threads_per_cta"] == shape["threads_per_cta"]
+    b.close()
+    b2.close()
+    for w in batch + alone:
+        w.close()
+
+
+def test_prepared_batch_refuses_a_world_too_large_for_a_cluster():
+    w = _world(160, 96, (0.0, 0.0, 1.0), 24, -1, 8)
+    with pytest.raises(swe.SweError) as e:
+        swe.Batch([w], [20000])
+    assert e.value.code == -1
+    w.close()

@@ -45,3 +45,41 @@ def test_replayed_graph_equals_direct_cycles(n, particles, lanes):
     graphed.set_stream(None)
     for w in (direct, graphed):
         w.close()
+
+
+def test_replayed_batch_graph_equals_direct_cycles():
+    """The prepared ensemble (swe_batch_run) captured once and replayed:
+    every replay is one more cycle of every world, bit for bit what each
+    world's own direct cycles give."""
+    torch = pytest.importorskip("torch")
+    cases = [(48, 48, 3000, WIND_101, 3), (64, 40, 2500, (0.0, 0.0, -1.0), 4), (96, 96, 9000, (1.0, 0.0, 0.0), 5)]
+
+    def world(n, nz, wind, sd):
+        h = (terrain.normalise(terrain.fbm(n, nz, sd, 4.0 / max(n, nz))) + 0.1).astype(np.float32)
+        w = swe.World(n, nz, params=swe.Params(pspeed=wind, frac_bits=16), seed=100 + sd)
+        w.upload(swe.Field.HEIGHT, h)
+        return w
+
+    graphed = [world(n, nz, wind, sd) for n, nz, _, wind, sd in cases]
+    direct = [world(n, nz, wind, sd) for n, nz, _, wind, sd in cases]
+    particles = [c[2] for c in cases]
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    graphed[0].set_stream(stream.cuda_stream)
+    b = swe.Batch(graphed, particles)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
+        b.run(1)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    for w, p in zip(direct, particles):
+        w.erode(p, 3, mode=swe.Mode.PARALLEL)
+    for k, (a, c) in enumerate(zip(graphed, direct)):
+        for f in swe.FIELDS:
+            assert np.array_equal(bits(a.download(f)), bits(c.download(f))), (k, f)
+        assert a.status() == 0
+    b.close()
+    graphed[0].set_stream(None)
+    for w in graphed + direct:
+        w.close()

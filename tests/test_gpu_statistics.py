@@ -18,29 +18,11 @@ import simplewinderosion_gb300 as swe
 from oracle import oracle
 from simplewinderosion_gb300 import terrain
 from tests.conftest import WIND_101
+from tests.terrain_stats import spec_dist, w1
 
 pytestmark = pytest.mark.gpu
 
 N, P, C = 256, 16384, 10
-
-
-def w1(a, b):
-    return float(np.mean(np.abs(np.sort(a.ravel()) - np.sort(b.ravel()))))
-
-
-def log_spectrum(a):
-    f = np.abs(np.fft.rfft2(a - a.mean())) ** 2
-    ky = np.fft.fftfreq(a.shape[0])[:, None]
-    kx = np.fft.rfftfreq(a.shape[1])[None, :]
-    k = np.sqrt(kx ** 2 + ky ** 2)
-    bins = np.linspace(0, 0.5, 33)
-    idx = np.digitize(k.ravel(), bins)
-    s = np.array([f.ravel()[idx == i].mean() if np.any(idx == i) else 0.0 for i in range(1, 33)])
-    return np.log10(s + 1e-12)
-
-
-def spec_dist(a, b):
-    return float(np.sqrt(np.mean((log_spectrum(a) - log_spectrum(b)) ** 2)))
 
 
 @pytest.fixture(scope="module")
