@@ -369,6 +369,31 @@ int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, const swe_p
  * multiple of 16, cout of 8. Runs on the tensor cores (implicit GEMM). */
 int swe_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int n, int h, int wd, int cin, int cout,
                    void* stream);
+/* The same convolution on the Blackwell tensor cores (tcgen05.mma, fp32
+ * accumulators in tensor memory, TMA-fed operand tiles, a 4-stage mbarrier
+ * pipeline). Weights come packed by swe_nn_conv3x3_tc_pack: flip == 0 packs
+ * w bf16 [cout,3,3,cin] for the forward convolution (x has cin channels, y
+ * cout); flip != 0 packs the flipped, transposed weights whose convolution
+ * of dy (cout channels) is the input gradient (cin channels), i.e. this call
+ * with cin and cout swapped. `act` (or NULL) also receives GELU(y), fused
+ * into the epilogue. cin and cout multiples of 16, cout <= 256; with TW the
+ * largest power of two up to 128 dividing the map width, TW >= 8 and the
+ * height a multiple of 128 / TW (a 128-pixel tile is 128 / TW rows of TW
+ * pixels); tensors 16-byte aligned. packed: 9*cin*cout bf16. */
+int swe_nn_conv3x3_tc_pack(const void* w, void* wp, int cin, int cout, int flip, void* stream);
+int swe_nn_conv3x3_tc(const void* x, const void* wp, const float* bias, void* y, void* act, int n, int h, int wd,
+                      int cin, int cout, void* stream);
+/* Weight and bias gradients of swe_nn_conv3x3 on the tensor cores, ADDED to
+ * dw (fp32 [cout,3,3,cin]) and db (fp32 [cout], or NULL): per tap a GEMM
+ * with M = output channels, N = input channels, K = pixels (split over
+ * CTAs, partial sums added with fp32 atomics). cin and cout multiples of 16
+ * up to 128; map shape as for swe_nn_conv3x3_tc; x and dy 16-byte aligned. */
+int swe_nn_conv3x3_wgrad_tc(const void* x, const void* dy, float* dw, float* db, int n, int h, int wd, int cin,
+                            int cout, void* stream);
+/* SWE_ERR_DEVICE (code in *status) if a tensor-core kernel gave up on a wait
+ * since the last call (each wait has a 2 s deadline); clears the code. Call
+ * after synchronising the streams the kernels ran on. */
+int swe_nn_status(uint32_t* status);
 /* wf[ci,2-di,2-dj,co] = w[co,di,dj,ci]: the weights whose convolution of dy
  * is the input gradient of swe_nn_conv3x3. */
 int swe_nn_conv3x3_flip(const void* w, void* wf, int cin, int cout, void* stream);

@@ -22,7 +22,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "libswe_oracle.so"
 REF_DIR = HERE / "_ref"
-REFERENCE_SRC = Path(os.environ.get("SWE_REFERENCE", "/root/reference"))
+# The reference checkout: $SWE_REFERENCE, else a directory named "reference"
+# beside this repository.
+REFERENCE_SRC = Path(os.environ.get("SWE_REFERENCE", str(HERE.parent.parent / "reference")))
 
 RNG_LIBC, RNG_GLIBC, RNG_TAPE = 0, 1, 2
 EXP_LIBM, EXP_CR = 0, 1

@@ -195,7 +195,7 @@ __device__ __forceinline__ float exp_libm(float x, const Consts& c) {
 }
 
 // (float)(1.0 - 0.3 * (double)s), the drag factor of Wind::fly
-// (wind.hpp:98: glm multiplies the speed by a double). For 0 <= s < 2 the
+// (wind.hpp:87: glm multiplies the speed by a double). For 0 <= s < 2 the
 // exact value 1 - 0.3d s (0.3d = Dhi + Dlo + 2^-52.4) is formed in float-
 // float arithmetic within 2^-47, and its nearest float is returned when it
 // lies more than 0.001 ulp (>= 2^-35) from a rounding midpoint: the double

@@ -157,6 +157,8 @@ cudaError_t nn_flip(const void* w, void* wf, int cin, int cout, cudaStream_t s);
 cudaError_t nn_conv_wgrad(const void* x, const void* dy, float* dw, float* db, int N, int H, int W, int cin, int cout,
                           cudaStream_t s);
 cudaError_t nn_gelu(const void* pre, void* act, long n, cudaStream_t s);
+// db (fp32 [cout]) += sum over the M pixels of dy (bf16 [M, cout]).
+cudaError_t nn_bias_grad(const void* dy, float* db, long M, int cout, cudaStream_t s);
 cudaError_t nn_gelu_bwd(const void* pre, const void* dact, void* dpre, long n, cudaStream_t s);
 cudaError_t nn_pool2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s);
 cudaError_t nn_up2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s);
@@ -168,5 +170,16 @@ cudaError_t nn_channel0(const void* pred, float* out, long M, int C, float oscal
 cudaError_t nn_adam(float* w, const float* grad, float* m, float* v, void* w16, long n, float lr, float b1, float b2,
                     float eps, int step, cudaStream_t s);
 cudaError_t nn_to_bf16(const float* a, void* b, long n, cudaStream_t s);
+// ---- tensor-core (tcgen05/TMEM/TMA) convolutions (swe_umma.cu) ----
+bool nn_conv_tc_supported(int H, int W, int kc, int nc);
+cudaError_t nn_pack_tc(const void* w, void* wp, int cin, int cout, bool flip, cudaStream_t s);
+cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y, void* act, int N, int H, int W,
+                       int kc, int nc, cudaStream_t s);
+bool nn_wgrad_tc_supported(int H, int W, int cin, int cout);
+// dw (fp32 [cout,3,3,cin]) += the weight gradient; sms: the device's SMs (sizes the split over pixels).
+cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, int W, int cin, int cout, int sms,
+                        cudaStream_t s);
+// The first error code a tensor-core kernel recorded since the last call (0: none); clears it.
+cudaError_t nn_tc_status(unsigned int* code);
 
 }  // namespace swe

@@ -522,6 +522,13 @@ cudaError_t nn_conv_wgrad(const void* x, const void* dy, float* dw, float* db, i
   return cudaGetLastError();
 }
 
+cudaError_t nn_bias_grad(const void* dy, float* db, long M, int cout, cudaStream_t s) {
+  long bx = (M + 255) / 256;
+  if (bx > 1024) bx = 1024;
+  k_bias_grad<<<(unsigned)bx, 256, 0, s>>>(static_cast<const bf16*>(dy), db, M, cout);
+  return cudaGetLastError();
+}
+
 cudaError_t nn_gelu(const void* pre, void* act, long n, cudaStream_t s) {
   k_gelu<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(pre), static_cast<bf16*>(act), n / 8);
   return cudaGetLastError();
@@ -620,6 +627,48 @@ int swe_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int
   if (!aligned16(x) || !aligned16(w) || !aligned4(y))
     return nn_fail(SWE_ERR_INVALID, "x and w must be 16-byte aligned, y 4-byte aligned");
   return nn_done(swe::nn_conv3x3(x, w, bias, y, n, h, wd, cin, cout, static_cast<cudaStream_t>(stream)));
+}
+
+int swe_nn_conv3x3_tc_pack(const void* w, void* wp, int cin, int cout, int flip, void* stream) {
+  if (!w || !wp || cin < 1 || cout < 1) return nn_fail(SWE_ERR_INVALID, "conv3x3_tc_pack: bad arguments");
+  return nn_done(swe::nn_pack_tc(w, wp, cin, cout, flip != 0, static_cast<cudaStream_t>(stream)));
+}
+
+int swe_nn_conv3x3_tc(const void* x, const void* wp, const float* bias, void* y, void* act, int n, int h, int wd,
+                      int cin, int cout, void* stream) {
+  if (!x || !wp || !y) return nn_fail(SWE_ERR_INVALID, "NULL tensor");
+  if (n < 1 || !swe::nn_conv_tc_supported(h, wd, cin, cout))
+    return nn_fail(SWE_ERR_INVALID,
+                   "conv3x3_tc: need cin % 16 == 0, cout % 16 == 0, cout <= 256, a width with a power-of-two "
+                   "factor TW >= 8 (up to 128) and a height that is a multiple of 128 / TW");
+  if (!aligned16(x) || !aligned16(wp) || !aligned16(y) || (act && !aligned16(act)))
+    return nn_fail(SWE_ERR_INVALID, "conv3x3_tc: tensors must be 16-byte aligned");
+  return nn_done(swe::nn_conv_tc(x, wp, bias, y, act, n, h, wd, cin, cout, static_cast<cudaStream_t>(stream)));
+}
+
+int swe_nn_conv3x3_wgrad_tc(const void* x, const void* dy, float* dw, float* db, int n, int h, int wd, int cin,
+                            int cout, void* stream) {
+  if (!x || !dy || !dw) return nn_fail(SWE_ERR_INVALID, "NULL tensor");
+  if (n < 1 || !swe::nn_wgrad_tc_supported(h, wd, cin, cout))
+    return nn_fail(SWE_ERR_INVALID,
+                   "conv3x3_wgrad_tc: need cin, cout multiples of 16 up to 128, a width with a power-of-two "
+                   "factor TW >= 8 (up to 128) and a height that is a multiple of 128 / TW");
+  if (!aligned16(x) || !aligned16(dy)) return nn_fail(SWE_ERR_INVALID, "tensors must be 16-byte aligned");
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return nn_fail(SWE_ERR_CUDA, "no current device");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = swe::nn_wgrad_tc(x, dy, dw, n, h, wd, cin, cout, sms, s);
+  if (e == cudaSuccess && db) e = swe::nn_bias_grad(dy, db, (long)n * h * wd, cout, s);
+  return nn_done(e);
+}
+
+int swe_nn_status(uint32_t* status) {
+  unsigned int v = 0;
+  if (int rc = nn_done(swe::nn_tc_status(&v))) return rc;
+  if (status) *status = v;
+  if (v) return nn_fail(SWE_ERR_DEVICE, "a tensor-core kernel gave up waiting (code " + std::to_string(v) + ")");
+  return SWE_OK;
 }
 
 int swe_nn_conv3x3_flip(const void* w, void* wf, int cin, int cout, void* stream) {

@@ -1,0 +1,642 @@
+// Blackwell tensor-core convolutions of the learned surrogate (sm_103a):
+// tcgen05.mma with the accumulators in tensor memory (TMEM), operand tiles
+// brought into shared memory by the tensor-memory accelerator (TMA), and a
+// multi-stage mbarrier pipeline.
+//
+//   k_conv_tc   3x3 convolution, zero padding, NHWC bf16, as an implicit
+//               GEMM: rows = 128-pixel tiles of the output (two per CTA),
+//               columns = output channels, K = 9 taps x input channels.
+//               Per k-block (one tap, 8*KG input channels) the TMA loads the
+//               tap-shifted 128-pixel tile of the input straight from the
+//               NHWC tensor (pixels beyond the map edge arrive as zeros: the
+//               padding costs nothing), and a bulk copy brings the matching
+//               slice of the pre-packed weights. One thread issues the MMAs,
+//               one thread the copies; all four warps run the epilogue
+//               (TMEM -> registers, + bias, optional fused GELU, bf16 stores).
+//               The input gradient is the same kernel on the output gradient
+//               with the weights flipped and transposed at packing time.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8x8 bf16 "core matrices" of 128 contiguous bytes, 8 rows of 16 bytes. A
+// TMA box of 8 channels x 128 pixels lands exactly as 16 such core matrices
+// stacked along M (the stride between them, SBO, is 128 bytes), and the next
+// 8 channels sit one box further on (LBO = 2048 bytes); the packed weights
+// are laid out the same way ([tap][channel group][n][8]).
+//
+// Every wait on an mbarrier is bounded (2 s by the global timer): past it the
+// kernel records an error code in g_tc_error, stops issuing work, waits
+// (bounded) for the copies it already issued, frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "swe_kernels.h"
+
+namespace swe {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+__device__ unsigned int g_tc_error;  // first failure code of a tensor-core kernel (0: none)
+
+constexpr int kTcThreads = 128;
+constexpr int kTcStages = 4;
+constexpr int kTcMTiles = 2;  // 128-pixel M tiles per CTA (they share each weight slice)
+constexpr unsigned long long kTcWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long tc_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase of `bar` with parity `parity`. Gives up when another
+// role of the CTA has given up (*abort != 0, if `watch`) or after the
+// deadline, recording `code`. Returns false if it gave up.
+__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, bool watch,
+                                       unsigned code) {
+  unsigned long long t0 = 0;
+  for (uint32_t i = 0;; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 31u) == 31u) {
+      if (watch && *abort) return false;
+      const unsigned long long now = tc_now();
+      if (t0 == 0) {
+        t0 = now;
+      } else if (now - t0 > kTcWaitNs) {
+        atomicCAS(&g_tc_error, 0u, code);
+        *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: start address, LBO (K direction), SBO
+// (M/N direction), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: bf16 A and B, fp32 D, both K-major,
+// M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// The same with both operands MN-major (the M or N index contiguous):
+// transpose bits 15 (A) and 16 (B).
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) { return idesc_bf16(m, n) | (1u << 15) | (1u << 16); }
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrives on `bar` once every MMA this thread issued before has completed.
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float gelu_erf(float v) { return 0.5f * v * (1.0f + erff(v * 0.70710678118654752f)); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
+struct TcConvGeom {
+  int H, W;
+  int kc;      // GEMM K channels (input channels of this convolution)
+  int nc;      // GEMM N (output channels)
+  int TW, R;   // an M tile: R image rows x TW pixels = 128 pixels
+  int KG;      // 8-channel groups per k-block
+  int chunks;  // kc / (8 KG)
+  int tiles;   // 128-pixel tiles in the batch
+  int col_stride;  // TMEM columns between the CTA's M tiles
+  int ncols;       // TMEM columns allocated
+  int stage_bytes, a_bytes;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_conv_tc(const __grid_constant__ CUtensorMap xmap, const bf16* __restrict__ wp, const float* __restrict__ bias,
+              bf16* __restrict__ y, bf16* __restrict__ act, const TcConvGeom g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTcStages * g.stage_bytes);
+  uint64_t* empty = full + kTcStages;
+  uint64_t* accum = empty + kTcStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* consumed = abort + 1;  // k-blocks whose data the MMA thread took
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile0 = blockIdx.x * kTcMTiles;
+  const int mt_n = min(kTcMTiles, g.tiles - tile0);
+  const int kblocks = 9 * g.chunks;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; s++) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(accum, 1);
+    *abort = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(g.ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int issued = 0;  // producer: k-blocks whose copies were issued
+  if (warp == 0 && lane == 0) {
+    // ---- producer: TMA for the shifted input tiles, bulk copy for the weights
+    const int tiles_per_img = (g.H * g.W) >> 7;
+    int tn[kTcMTiles], ty[kTcMTiles], tx[kTcMTiles];
+#pragma unroll
+    for (int mt = 0; mt < kTcMTiles; mt++) {
+      const int t = tile0 + mt;
+      const int q = t % tiles_per_img;
+      tn[mt] = t / tiles_per_img;
+      ty[mt] = (q / (g.W / g.TW)) * g.R;
+      tx[mt] = (q % (g.W / g.TW)) * g.TW;
+    }
+    const uint32_t b_bytes = (uint32_t)g.KG * g.nc * 16;
+    const uint32_t bytes = (uint32_t)mt_n * g.KG * 2048 + b_bytes;
+    for (int kb = 0; kb < kblocks; kb++) {
+      const int s = kb % kTcStages;
+      const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
+      if (!mbar_wait(empty + s, ph ^ 1u, abort, true, 1u)) break;
+      const int tap = kb / g.chunks, chunk = kb % g.chunks;
+      const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+      unsigned char* st = smem + s * g.stage_bytes;
+      mbar_expect_tx(full + s, bytes);
+      for (int mt = 0; mt < mt_n; mt++)
+        for (int k = 0; k < g.KG; k++)
+          tma_load_4d(st + (mt * g.KG + k) * 2048, &xmap, full + s, (chunk * g.KG + k) * 8, tx[mt] + dx,
+                      ty[mt] + dy, tn[mt]);
+      bulk_load(st + g.a_bytes, wp + ((size_t)tap * g.kc + (size_t)chunk * g.KG * 8) * g.nc, b_bytes, full + s);
+      issued = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    const uint32_t idesc = idesc_bf16(128, g.nc);
+    const uint32_t sb = smem_u32(smem);
+    int kb = 0;
+    for (; kb < kblocks; kb++) {
+      const int s = kb % kTcStages;
+      const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
+      if (!mbar_wait(full + s, ph, abort, true, 2u)) break;
+      tc_fence_after();
+      const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + g.a_bytes;
+      for (int mt = 0; mt < mt_n; mt++) {
+        for (int j = 0; j < g.KG / 2; j++) {
+          const uint64_t ad = smem_desc(a0 + (mt * g.KG + 2 * j) * 2048, 2048, 128);
+          const uint64_t bd = smem_desc(b0 + 2 * j * g.nc * 16, g.nc * 16, 128);
+          umma_bf16(tmem + mt * g.col_stride, ad, bd, idesc, (kb > 0 || j > 0) ? 1u : 0u);
+        }
+      }
+      umma_commit(empty + s);  // the stage is free once these MMAs have read it
+    }
+    *consumed = kb;
+    umma_commit(accum);  // every MMA issued, done or not, before the accumulators are read
+  }
+
+  // ---- epilogue: all four warps, warp w reads TMEM lanes 32w..32w+31
+  __syncwarp();
+  const bool have = mbar_wait(accum, 0u, abort, false, 3u);
+  tc_fence_after();
+  // warp-uniform: the TMEM loads below are .sync.aligned
+  if (__all_sync(0xffffffffu, have && *abort == 0)) {
+    for (int mt = 0; mt < mt_n; mt++) {
+      // TMEM lane l of the tile is image pixel (ty + l / TW, tx + l % TW)
+      const int t = tile0 + mt, tiles_per_img = (g.H * g.W) >> 7;
+      const int q = t % tiles_per_img, l = warp * 32 + lane;
+      const long pix = ((long)(t / tiles_per_img) * g.H + (q / (g.W / g.TW)) * g.R + l / g.TW) * g.W +
+                       (q % (g.W / g.TW)) * g.TW + l % g.TW;
+      for (int j = 0; j < g.nc / 16; j++) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + mt * g.col_stride + 16 * j, v);
+        if (bias) {
+#pragma unroll
+          for (int i = 0; i < 16; i++) v[i] += bias[16 * j + i];
+        }
+        uint4 o0, o1;
+        o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
+        o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
+        o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
+        o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
+        uint4* dst = reinterpret_cast<uint4*>(y + pix * g.nc + 16 * j);
+        dst[0] = o0;
+        dst[1] = o1;
+        if (act) {
+          // GELU of the bf16-rounded pre-activation, as the separate GELU pass computes it
+#pragma unroll
+          for (int i = 0; i < 16; i++) v[i] = gelu_erf(__bfloat162float(__float2bfloat16_rn(v[i])));
+          o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
+          o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
+          o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
+          o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
+          uint4* da = reinterpret_cast<uint4*>(act + pix * g.nc + 16 * j);
+          da[0] = o0;
+          da[1] = o1;
+        }
+      }
+    }
+  }
+
+  // ---- teardown: no copy may land after the CTA exits, and TMEM is freed
+  __syncthreads();  // the MMA thread's count of consumed k-blocks is visible
+  if (warp == 0 && lane == 0) {
+    for (int kb = *consumed; kb < issued; kb++)
+      mbar_wait(full + kb % kTcStages, (uint32_t)(kb / kTcStages) & 1u, abort, false, 4u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.ncols) : "memory");
+}
+
+struct TcWgradGeom {
+  int H, W, cin, cout;
+  int TW, R;          // an M tile: R image rows x TW pixels = 128 pixels
+  int tiles;          // 128-pixel tiles in the batch
+  int tiles_per_cta;  // the CTA's share of the pixel sum (split K)
+  int taps;           // taps per CTA (9, or 3: one row of taps per blockIdx.y)
+  int col_stride;     // TMEM columns per tap
+  int ncols;
+  int stages;
+  int a_bytes, stage_bytes;
+  int tail;  // bytes after the stages: the 128 padded M rows of the last stage's A stay in the allocation
+};
+
+// Weight gradient dW[co][tap][ci] += sum over pixels p of dy[p][co] x[p + tap][ci]
+// as a GEMM per tap with M = output channels (padded to 128; the rows past
+// cout are never stored), N = input channels, K = pixels, split over CTAs by
+// pixel tiles and over blockIdx.y by rows of taps. Both operands are
+// MN-major in shared memory (channels contiguous): a TMA box of 8 channels x
+// 128 pixels is 16 core matrices along K (LBO = 128 bytes) and the next 8
+// channels sit one box further on (SBO = 2048 bytes). Per k-block (one pixel
+// tile, one tap) the TMA brings the dy tile and the tap-shifted x tile
+// (zeros past the map edge). The partial sums leave TMEM through fp32
+// atomics into dw.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap,
+               float* __restrict__ dw, const TcWgradGeom g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  // stages, then a tail that keeps the padded M rows of the last stage's A
+  // operand inside the allocation, then the barriers
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + g.stages * g.stage_bytes + g.tail);
+  uint64_t* empty = full + 4;
+  uint64_t* accum = empty + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* consumed = abort + 1;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t0 = blockIdx.x * g.tiles_per_cta;
+  const int nt = max(0, min(g.tiles_per_cta, g.tiles - t0));
+  const int tap0 = blockIdx.y * g.taps;
+  const int kblocks = nt * g.taps;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < g.stages; s++) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(accum, 1);
+    *abort = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(g.ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    const int tiles_per_img = (g.H * g.W) >> 7;
+    const uint32_t bytes = (uint32_t)(g.cout / 8 + g.cin / 8) * 2048;
+    for (int kb = 0; kb < kblocks; kb++) {
+      const int s = kb % g.stages;
+      const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
+      if (!mbar_wait(empty + s, ph ^ 1u, abort, true, 11u)) break;
+      const int t = t0 + kb / g.taps, tap = tap0 + kb % g.taps;
+      const int q = t % tiles_per_img, tn = t / tiles_per_img;
+      const int ty = (q / (g.W / g.TW)) * g.R, tx = (q % (g.W / g.TW)) * g.TW;
+      const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+      unsigned char* st = smem + s * g.stage_bytes;
+      mbar_expect_tx(full + s, bytes);
+      for (int k = 0; k < g.cout / 8; k++) tma_load_4d(st + k * 2048, &dymap, full + s, 8 * k, tx, ty, tn);
+      for (int k = 0; k < g.cin / 8; k++)
+        tma_load_4d(st + g.a_bytes + k * 2048, &xmap, full + s, 8 * k, tx + dx, ty + dy, tn);
+      issued = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    const uint32_t idesc = idesc_bf16_mn(128, g.cin);
+    const uint32_t sb = smem_u32(smem);
+    int kb = 0;
+    for (; kb < kblocks; kb++) {
+      const int s = kb % g.stages;
+      const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
+      if (!mbar_wait(full + s, ph, abort, true, 12u)) break;
+      tc_fence_after();
+      const int i = kb / g.taps, j = kb % g.taps;
+      const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + g.a_bytes;
+#pragma unroll
+      for (int k16 = 0; k16 < 8; k16++) {
+        const uint64_t ad = smem_desc(a0 + 256 * k16, 128, 2048);
+        const uint64_t bd = smem_desc(b0 + 256 * k16, 128, 2048);
+        umma_bf16(tmem + j * g.col_stride, ad, bd, idesc, (i > 0 || k16 > 0) ? 1u : 0u);
+      }
+      umma_commit(empty + s);
+    }
+    *consumed = kb;
+    umma_commit(accum);
+  }
+
+  __syncwarp();
+  const bool have = mbar_wait(accum, 0u, abort, false, 13u);
+  tc_fence_after();
+  if (__all_sync(0xffffffffu, have && *abort == 0) && nt > 0) {
+    const int co = warp * 32 + lane;  // TMEM lane = output channel
+    for (int j = 0; j < g.taps; j++) {
+      for (int c16 = 0; c16 < g.cin / 16; c16++) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + j * g.col_stride + 16 * c16, v);
+        if (co < g.cout) {
+          float* dst = dw + ((long)co * 9 + tap0 + j) * g.cin + 16 * c16;
+#pragma unroll
+          for (int i = 0; i < 16; i++) atomicAdd(dst + i, v[i]);
+        }
+      }
+    }
+  }
+
+  __syncthreads();
+  if (warp == 0 && lane == 0) {
+    for (int kb = *consumed; kb < issued; kb++)
+      mbar_wait(full + kb % g.stages, (uint32_t)(kb / g.stages) & 1u, abort, false, 14u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.ncols) : "memory");
+}
+
+// Packed weights of a convolution for k_conv_tc: wp[tap][k/8][n][k%8] with
+// K the convolution's input channels and N its output channels. Forward:
+// w[n][tap][k] (w bf16 [cout][3][3][cin]). Input gradient (flip): the
+// convolution of dy with the flipped, transposed weights, K = cout, N = cin:
+// w[k][8 - tap][n].
+__global__ void k_pack_tc(const bf16* __restrict__ w, bf16* __restrict__ wp, int cin, int cout, int flip) {
+  const int kc = flip ? cout : cin, nc = flip ? cin : cout;
+  const long total = 9l * kc * nc;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int tap = (int)(i / ((long)kc * nc));
+    const int rem = (int)(i % ((long)kc * nc));
+    const int gk = rem / (nc * 8);
+    const int r2 = rem % (nc * 8);
+    const int n = r2 >> 3, k = gk * 8 + (r2 & 7);
+    wp[i] = flip ? w[((long)k * 9 + (8 - tap)) * cin + n] : w[((long)n * 9 + tap) * cin + k];
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, []() {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+}  // namespace
+
+// Width of a 128-pixel M tile: the largest power of two up to 128 dividing
+// the map width (a tile is 128 / TW rows of TW pixels).
+static int tile_width(int W) {
+  int tw = 128;
+  while (tw > 1 && W % tw != 0) tw >>= 1;
+  return tw;
+}
+
+bool nn_conv_tc_supported(int H, int W, int kc, int nc) {
+  if (kc < 16 || kc % 16 != 0 || nc < 16 || nc % 16 != 0 || nc > 256) return false;
+  const int TW = tile_width(W);
+  return TW >= 8 && H % (128 / TW) == 0;
+}
+
+cudaError_t nn_pack_tc(const void* w, void* wp, int cin, int cout, bool flip, cudaStream_t s) {
+  const long total = 9l * cin * cout;
+  const int grid = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
+  k_pack_tc<<<grid, 256, 0, s>>>(static_cast<const bf16*>(w), static_cast<bf16*>(wp), cin, cout, flip ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y, void* act, int N, int H, int W,
+                       int kc, int nc, cudaStream_t s) {
+  if (!nn_conv_tc_supported(H, W, kc, nc)) return cudaErrorNotSupported;
+  if ((reinterpret_cast<uintptr_t>(x) & 15) || (reinterpret_cast<uintptr_t>(wp) & 15) ||
+      (reinterpret_cast<uintptr_t>(y) & 15) || (act && (reinterpret_cast<uintptr_t>(act) & 15)))
+    return cudaErrorMisalignedAddress;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  TcConvGeom g;
+  g.H = H;
+  g.W = W;
+  g.kc = kc;
+  g.nc = nc;
+  g.TW = tile_width(W);
+  g.R = 128 / g.TW;
+  g.KG = (kc / 8) % 4 == 0 ? 4 : 2;
+  g.chunks = kc / (8 * g.KG);
+  const long pixels = (long)N * H * W;
+  g.tiles = (int)(pixels / 128);
+  g.col_stride = (nc + 31) / 32 * 32;
+  int cols = 32;
+  while (cols < kTcMTiles * g.col_stride) cols <<= 1;
+  g.ncols = cols;
+  g.a_bytes = kTcMTiles * g.KG * 2048;
+  g.stage_bytes = (g.a_bytes + g.KG * nc * 16 + 1023) / 1024 * 1024;
+  const size_t smem = 1024 + (size_t)kTcStages * g.stage_bytes + (2 * kTcStages + 1) * 8 + 16;
+
+  CUtensorMap map;
+  const cuuint64_t dims[4] = {(cuuint64_t)kc, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t strides[3] = {(cuuint64_t)kc * 2, (cuuint64_t)W * kc * 2, (cuuint64_t)H * W * kc * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int grid = (g.tiles + kTcMTiles - 1) / kTcMTiles;
+  k_conv_tc<<<grid, kTcThreads, smem, s>>>(map, static_cast<const bf16*>(wp), bias, static_cast<bf16*>(y),
+                                           static_cast<bf16*>(act), g);
+  return cudaGetLastError();
+}
+
+namespace {
+
+// NHWC bf16 tensor map with boxes of 8 channels x (TW pixels x R rows).
+cudaError_t nhwc_map(CUtensorMap* map, const void* t, int N, int H, int W, int C, int TW, int R) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)TW, (cuuint32_t)R, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(t), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+bool nn_wgrad_tc_supported(int H, int W, int cin, int cout) {
+  return nn_conv_tc_supported(H, W, cin, cin) && cout >= 16 && cout % 16 == 0 && cout <= 128 && cin <= 128;
+}
+
+cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, int W, int cin, int cout, int sms,
+                        cudaStream_t s) {
+  if (!nn_wgrad_tc_supported(H, W, cin, cout)) return cudaErrorNotSupported;
+  if ((reinterpret_cast<uintptr_t>(x) & 15) || (reinterpret_cast<uintptr_t>(dy) & 15)) return cudaErrorMisalignedAddress;
+  TcWgradGeom g;
+  g.H = H;
+  g.W = W;
+  g.cin = cin;
+  g.cout = cout;
+  g.TW = tile_width(W);
+  g.R = 128 / g.TW;
+  g.tiles = (int)((long)N * H * W / 128);
+  g.col_stride = (cin + 31) / 32 * 32;
+  g.taps = 9 * g.col_stride <= 512 ? 9 : 3;
+  int cols = 32;
+  while (cols < g.taps * g.col_stride) cols <<= 1;
+  g.ncols = cols;
+  g.a_bytes = cout / 8 * 2048;
+  g.stage_bytes = g.a_bytes + cin / 8 * 2048;
+  // the MMA reads 128 rows of A (16 channel groups x 2048 bytes) from each stage
+  g.tail = g.stage_bytes < 32768 ? 32768 - g.stage_bytes : 0;
+  g.stages = 4;
+  while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128 > 200 * 1024) g.stages--;
+  const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;
+  // about two CTAs per SM in all, each summing a run of pixel tiles
+  const int groups = 9 / g.taps;
+  int ctas_x = (2 * (sms > 0 ? sms : 148)) / groups;
+  if (ctas_x < 1) ctas_x = 1;
+  if (ctas_x > g.tiles) ctas_x = g.tiles;
+  g.tiles_per_cta = (g.tiles + ctas_x - 1) / ctas_x;
+  ctas_x = (g.tiles + g.tiles_per_cta - 1) / g.tiles_per_cta;
+  CUtensorMap xm, dm;
+  cudaError_t e = nhwc_map(&xm, x, N, H, W, cin, g.TW, g.R);
+  if (e == cudaSuccess) e = nhwc_map(&dm, dy, N, H, W, cout, g.TW, g.R);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_wgrad_tc<<<dim3(ctas_x, groups), kTcThreads, smem, s>>>(xm, dm, dw, g);
+  return cudaGetLastError();
+}
+
+cudaError_t nn_tc_status(unsigned int* code) {
+  unsigned int v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(v));
+  if (e == cudaSuccess && v) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(zero));
+  }
+  *code = v;
+  return e;
+}
+
+}  // namespace swe

@@ -44,6 +44,10 @@ def _bind():
     i64, f32, i32 = ctypes.c_int64, ctypes.c_float, ctypes.c_int
     L.swe_nn_conv3x3.argtypes = [_P, _P, _P, _P, i32, i32, i32, i32, i32, _P]
     L.swe_nn_conv3x3_flip.argtypes = [_P, _P, i32, i32, _P]
+    L.swe_nn_conv3x3_tc_pack.argtypes = [_P, _P, i32, i32, i32, _P]
+    L.swe_nn_conv3x3_tc.argtypes = [_P, _P, _P, _P, _P, i32, i32, i32, i32, i32, _P]
+    L.swe_nn_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    L.swe_nn_conv3x3_wgrad_tc.argtypes = [_P, _P, _P, _P, i32, i32, i32, i32, i32, _P]
     L.swe_nn_conv3x3_wgrad.argtypes = [_P, _P, _P, _P, i32, i32, i32, i32, i32, _P]
     L.swe_nn_gelu.argtypes = [_P, _P, i64, _P]
     L.swe_nn_gelu_bwd.argtypes = [_P, _P, _P, i64, _P]
@@ -82,6 +86,45 @@ class Ops:
         y = self.empty(n, h, wd, cout)
         _check(lib.swe_nn_conv3x3(_p(x), _p(w16), _p(b), _p(y), n, h, wd, cin, cout, self.s))
         return y
+
+    def pack_tc(self, w16, flip=False):
+        """Weights [cout,3,3,cin] packed for the tensor-core convolution
+        (flip: for the input gradient)."""
+        cout, _, _, cin = w16.shape
+        wp = self.empty(9 * cin * cout)
+        _check(lib.swe_nn_conv3x3_tc_pack(_p(w16), _p(wp), cin, cout, 1 if flip else 0, self.s))
+        return wp
+
+    def conv_tc(self, x, wp, b, cout, act=False):
+        """Tensor-core convolution of x with packed weights; with act, also
+        returns GELU of the output (fused into the epilogue)."""
+        n, h, wd, cin = x.shape
+        y = self.empty(n, h, wd, cout)
+        a = self.empty(n, h, wd, cout) if act else None
+        _check(lib.swe_nn_conv3x3_tc(_p(x), _p(wp), _p(b), _p(y), _p(a), n, h, wd, cin, cout, self.s))
+        return (y, a) if act else y
+
+    def wgrad_tc(self, x, dy, dw, db):
+        """Tensor-core weight gradient (and bias gradient) ADDED to dw, db."""
+        n, h, wd, cin = x.shape
+        _check(lib.swe_nn_conv3x3_wgrad_tc(_p(x), _p(dy), _p(dw), _p(db), n, h, wd, cin, dy.shape[3], self.s))
+
+    @staticmethod
+    def tc_ok(h, wd, cin, cout) -> bool:
+        """Whether the tensor-core convolution takes this shape."""
+        if cin % 16 or cout % 16 or cout > 256 or cin < 16 or cout < 16:
+            return False
+        tw = 128
+        while tw > 1 and wd % tw:
+            tw //= 2
+        return tw >= 8 and h % (128 // tw) == 0
+
+    def status(self) -> int:
+        """Raises if a tensor-core kernel gave up on a wait (synchronises)."""
+        self.torch.cuda.synchronize(self.device)
+        v = ctypes.c_uint32()
+        _check(lib.swe_nn_status(ctypes.byref(v)))
+        return v.value
 
     def conv_dx(self, dy, w16, cin):
         n, h, wd, cout = dy.shape
@@ -145,9 +188,10 @@ class Surrogate:
     """The U-Net, its fp32 master weights, bf16 copies, gradients and Adam
     moments. `scale`: the height change is predicted as change * scale."""
 
-    def __init__(self, device="cuda", seed=0, scale=100.0):
+    def __init__(self, device="cuda", seed=0, scale=100.0, use_tc=True):
         import torch
         self.torch = torch
+        self.use_tc = use_tc  # tensor-core (tcgen05) convolutions where the shape allows
         self.device = torch.device(device)
         self.ops = Ops(torch, self.device)
         self.scale = float(scale)
@@ -171,6 +215,7 @@ class Surrogate:
         self.sync_bf16()
 
     def sync_bf16(self):
+        self._packed = {}
         for k, w in self.w.items():
             if k not in self.w16:
                 self.w16[k] = self.ops.empty(*w.shape)
@@ -190,6 +235,39 @@ class Surrogate:
             self.b[k].copy_(self.torch.from_numpy(np.asarray(state[f"b_{k}"], np.float32)))
         self.sync_bf16()
 
+    # ---- the convolutions: tensor-core kernels where the shape allows ----
+    def _packed_w(self, name, flip):
+        key = (name, flip)
+        if key not in self._packed:
+            self._packed[key] = self.ops.pack_tc(self.w16[name], flip)
+        return self._packed[key]
+
+    def _conv(self, name, inp, act):
+        """(pre, GELU(pre)) with act, else pre."""
+        o = self.ops
+        n, h, wd, cin = inp.shape
+        cout = self.b[name].numel()
+        if self.use_tc and o.tc_ok(h, wd, cin, cout):
+            return o.conv_tc(inp, self._packed_w(name, False), self.b[name], cout, act=act)
+        pre = o.conv(inp, self.w16[name], self.b[name], cout)
+        return (pre, o.gelu(pre)) if act else pre
+
+    def _conv_dx(self, name, dy, cin):
+        o = self.ops
+        n, h, wd, cout = dy.shape
+        if self.use_tc and o.tc_ok(h, wd, cout, cin):
+            return o.conv_tc(dy, self._packed_w(name, True), None, cin)
+        return o.conv_dx(dy, self.w16[name], cin)
+
+    def _wgrad(self, name, inp, dy):
+        o = self.ops
+        n, h, wd, cin = inp.shape
+        cout = dy.shape[3]
+        if self.use_tc and o.tc_ok(h, wd, cin, cin) and cout % 16 == 0 and cout <= 128 and cin <= 128:
+            o.wgrad_tc(inp, dy, self.gw[name], self.gb[name])
+        else:
+            o.wgrad(inp, dy, self.gw[name], self.gb[name])
+
     # ---- forward / backward ----
     def forward(self, x):
         """x: bf16 [n,h,w,16]. Returns the output tensor [n,h,w,16] and the
@@ -198,9 +276,9 @@ class Surrogate:
         cache = {}
 
         def conv_act(name, inp):
-            pre = o.conv(inp, self.w16[name], self.b[name], self.b[name].numel())
+            pre, act = self._conv(name, inp, True)
             cache[name] = (inp, pre)
-            return o.gelu(pre)
+            return act
 
         a_in = conv_act("in", x)
         s0 = conv_act("e0", a_in)
@@ -211,7 +289,7 @@ class Surrogate:
         d2 = o.add(conv_act("u2", o.up(b3)), s2)
         d1 = o.add(conv_act("u1", o.up(d2)), s1)
         d0 = o.add(conv_act("u0", o.up(d1)), s0)
-        out = o.conv(d0, self.w16["out"], self.b["out"], 16)
+        out = self._conv("out", d0, False)
         cache["out"] = (d0, out)
         return out, cache
 
@@ -219,14 +297,14 @@ class Surrogate:
         """Adds the gradients of every weight and bias from d loss / d out."""
         o = self.ops
         d0, _ = cache["out"]
-        o.wgrad(d0, dout, self.gw["out"], self.gb["out"])
-        dd0 = o.conv_dx(dout, self.w16["out"], 32)
+        self._wgrad("out", d0, dout)
+        dd0 = self._conv_dx("out", dout, 32)
 
         def back(name, dact):
             inp, pre = cache[name]
             dpre = o.gelu_bwd(pre, dact)
-            o.wgrad(inp, dpre, self.gw[name], self.gb[name])
-            return o.conv_dx(dpre, self.w16[name], inp.shape[3]) if name != "in" else None
+            self._wgrad(name, inp, dpre)
+            return self._conv_dx(name, dpre, inp.shape[3]) if name != "in" else None
 
         dd1 = o.up_bwd(back("u0", dd0))
         dd2 = o.up_bwd(back("u1", dd1))
@@ -251,6 +329,7 @@ class Surrogate:
                                    self.w[k].numel(), lr, b1, b2, eps, self.t, s))
             _check(lib.swe_nn_adam(_p(self.b[k]), _p(self.gb[k]), _p(self.mb[k]), _p(self.vb[k]), None,
                                    self.b[k].numel(), lr, b1, b2, eps, self.t, s))
+        self._packed = {}  # the bf16 weights changed
 
     # ---- training and prediction ----
     def train_step(self, height, wind_xz, target_dh, lr=1e-3):
@@ -332,6 +411,44 @@ def make_pairs(count, size=256, cycles=50, particles=1000, seed=0, chunk=2048, m
             dh[first + i] = w.height - h0[first + i]
             w.close()
     return h0, wind, dh
+
+
+def predict_tiled(model: "Surrogate", h, wind_xz, tile: int = 256, halo: int = 32, batch: int = 16):
+    """The surrogate's height change for a large map h [n, n] (float32,
+    host), applied in tile x tile pieces, each predicted from a window with
+    `halo` cells of context on every side that the map has (windows at the
+    map edge are shifted inward so that they stay tile + 2 halo wide; the
+    map's own edge is then the window's edge, as in training). Only each
+    window's central tile is kept."""
+    torch = model.torch
+    nx, nz = h.shape
+    win = tile + 2 * halo
+    if nx < win or nz < win:
+        return predict_map_whole(model, h, wind_xz)
+    out = np.empty((nx, nz), np.float32)
+    jobs = []
+    for x0 in range(0, nx, tile):
+        for z0 in range(0, nz, tile):
+            wx0 = min(max(x0 - halo, 0), nx - win)
+            wz0 = min(max(z0 - halo, 0), nz - win)
+            jobs.append((x0, z0, wx0, wz0))
+    for k in range(0, len(jobs), batch):
+        part = jobs[k:k + batch]
+        hb = np.stack([h[wx0:wx0 + win, wz0:wz0 + win] for _, _, wx0, wz0 in part]).astype(np.float32)
+        wd = torch.tensor([list(wind_xz)] * len(part), dtype=torch.float32, device=model.device)
+        pred = model.predict(torch.from_numpy(hb).to(model.device), wd).cpu().numpy()
+        for (x0, z0, wx0, wz0), p in zip(part, pred):
+            tx, tz = min(tile, nx - x0), min(tile, nz - z0)
+            out[x0:x0 + tx, z0:z0 + tz] = p[x0 - wx0:x0 - wx0 + tx, z0 - wz0:z0 - wz0 + tz]
+    return out
+
+
+def predict_map_whole(model: "Surrogate", h, wind_xz):
+    """The surrogate's height change for one whole map h (float32, host)."""
+    torch = model.torch
+    hd = torch.from_numpy(np.ascontiguousarray(h[None], np.float32)).to(model.device)
+    wd = torch.tensor([list(wind_xz)], dtype=torch.float32, device=model.device)
+    return model.predict(hd, wd)[0].cpu().numpy()
 
 
 def rmse(a, b) -> float:

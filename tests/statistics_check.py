@@ -94,10 +94,13 @@ def main():
             t1 = time.time()
             w.erode(particles, 1, mode=swe.Mode.PARALLEL)
             dt = time.time() - t1
-            gw, gs, gm = gpu_distances(w.height, prof, spec, mean, c)
+            g = w.height
+            gw, gs, gm = gpu_distances(g, prof, spec, mean, c)
             nw, ns, nm = floors(prof, spec, mean, c)
+            signed = float(np.mean(g, dtype=np.float64)) - float(mean[:, c].mean())
             print(f"lanes {lanes:>8} cycle {c + 1}: W1 {gw:.6f} ({gw / nw:.2f}x)  spectrum {gs:.5f} "
-                  f"({gs / ns:.2f}x)  mean {gm:.6f} ({gm / max(nm, 1e-12):.2f}x)  [{dt * 1e3:.0f} ms]")
+                  f"({gs / ns:.2f}x)  mean {gm:.6f} ({gm / max(nm, 1e-12):.2f}x, GPU - reference average "
+                  f"{signed:+.6f})  [{dt * 1e3:.0f} ms]")
         m, inflight, e = w.mass_ledger()
         print(f"lanes {lanes:>8}: ledger map+exported-initial = {m + e - m0} (0 = exact)")
         w.close()

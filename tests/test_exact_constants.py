@@ -5,11 +5,13 @@ exp_ff (hi = nearest float, lo = nearest float to the rest, pair within
 significant bits, so k times them is exact for |k| < 2^13), 64/ln2, the
 Taylor coefficients, and the split of the double 0.3 used by drag_factor."""
 import math
+import os
 import re
 from decimal import Decimal, getcontext
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 SRC = (Path(__file__).resolve().parents[1] / "simplewinderosion_gb300" / "csrc" / "swe_device.cuh").read_text()
 getcontext().prec = 60
@@ -112,3 +114,21 @@ def test_drag_fast_path_equals_the_double_expression():
     # tenth of an ulp grid away from a rounding midpoint by 1e-17 or less, a
     # tie that only the double expression's own roundings decide.
     assert ok.mean() > 0.95
+
+
+@pytest.mark.skipif(not os.environ.get("SWE_EXHAUSTIVE"), reason="opt-in: SWE_EXHAUSTIVE=1 (about two minutes)")
+def test_drag_fast_path_exhaustive_over_zero_to_two():
+    """Every float in [0, 2) (bit patterns 0 .. 0x3FFFFFFF), in chunks of
+    2^24: where the fast path claims its result, it equals the double
+    expression (float)(1 - 0.3 * (double)s).
+
+        SWE_EXHAUSTIVE=1 python -m pytest tests/test_exact_constants.py -k exhaustive
+    """
+    claimed = 0
+    for first in range(0, 0x40000000, 1 << 24):
+        s = np.arange(first, first + (1 << 24), dtype=np.uint32).view(np.float32)
+        ok, fast = _drag_fast(s)
+        want = (1.0 - 0.3 * s.astype(np.float64)).astype(np.float32)
+        assert np.array_equal(fast[ok].view(np.uint32), want[ok].view(np.uint32)), hex(first)
+        claimed += int(ok.sum())
+    assert claimed > 0.99 * 0x40000000
