@@ -79,7 +79,7 @@ typedef enum swe_field {
  *            reference's results bit for bit. One GPU thread; a parity mode.
  *  PARALLEL: the particles of a cycle fly in lock-step steps, at most
  *            `lanes` of them at a time; a lane whose particle dies takes the
- *            cycle's next particle (lanes = 0: max(1024, nx*nz/64), which
+ *            cycle's next particle (lanes = 0: max(1024, nx*nz/256), which
  *            keeps the terrain statistics of the sequential reference;
  *            lanes < 0: all particles at once, fastest, statistically
  *            further from the reference). In a step every particle flies

@@ -679,7 +679,7 @@ int so_par_lanes(int lanes, int nx, int nz, int particles) {
   long l;
   if (lanes > 0) l = lanes;
   else if (lanes == 0) {
-    l = (long)nx * nz / 64;
+    l = (long)nx * nz / 256;
     if (l < 1024) l = 1024;
   } else l = particles;
   if (l > particles) l = particles;

@@ -68,7 +68,7 @@ void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out);
 /* --- CPU model of the parallel fixed-point mode (bitwise model of the GPU
  *     kernels: same float operation order, same counter-based RNG). --- */
 void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_t* cycle_counter);
-/* Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/64),
+/* Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/256),
  * < 0 -> all particles of the cycle; never more than the cycle's particles. */
 int so_par_lanes(int lanes, int nx, int nz, int particles);
 void so_par_get_heights_q(so_world* w, int32_t* dst);

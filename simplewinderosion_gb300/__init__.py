@@ -75,8 +75,8 @@ class Params:
     World::lrate/maxdiff/settling (world.hpp:30-32), quad::mapscale
     (cellpool.h:184), Wind::pspeed (wind.hpp:13). frac_bits is the parallel
     mode's fixed-point resolution; lanes its particles in flight (0: automatic,
-    max(1024, cells/64), which keeps the sequential reference's terrain
-    statistics; < 0: all particles of a cycle at once)."""
+    max(1024, cells/256), which keeps the sequential reference's terrain
+    statistics: height histogram, spectrum and mean; < 0: all particles of a cycle at once)."""
 
     max_age: int = 512
     boundarylayer: float = 2.0

@@ -82,7 +82,7 @@ bool lanes_form_fits(int lanes, long n);
 // Sets the cycle counter (which keys the parallel mode's random numbers) on
 // the device, in stream order.
 void launch_set_cycle(Counters* cnt, uint64_t cycle, cudaStream_t s);
-// Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/64),
+// Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/256),
 // < 0 -> all particles of the cycle; never more than the cycle's particles.
 int par_lanes(int lanes, int nx, int nz, int particles);
 void launch_sum_fixed(const int32_t* hq, long n, long long* out, cudaStream_t s);

@@ -1640,7 +1640,7 @@ int par_lanes(int lanes, int nx, int nz, int particles) {
   if (lanes > 0) {
     l = lanes;
   } else if (lanes == 0) {
-    l = (long)nx * nz / 64;
+    l = (long)nx * nz / 256;
     if (l < 1024) l = 1024;
   } else {
     l = particles;

@@ -329,24 +329,25 @@ __global__ void k_gelu_bwd(const bf16* __restrict__ pre, const bf16* __restrict_
 }
 
 // y[n][i][j][c] = mean of x[n][2i..2i+1][2j..2j+1][c] (H, W even: the input's).
+template <class I>
 __global__ void k_pool2(const bf16* __restrict__ x, bf16* __restrict__ y, int N, int H, int W, int C) {
   const int Ho = H / 2, Wo = W / 2, G = C / 8;
-  const long n = (long)N * Ho * Wo * G;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  const I n = (I)N * Ho * Wo * G;
+  for (I i = blockIdx.x * (I)blockDim.x + threadIdx.x; i < n; i += (I)gridDim.x * blockDim.x) {
     const int c = (int)(i % G) * 8;
-    const long q = i / G;
+    const I q = i / G;
     const int j = (int)(q % Wo), ii = (int)((q / Wo) % Ho);
-    const long b = q / ((long)Wo * Ho);
-    const long s = ((b * H + 2 * ii) * W + 2 * j) * C + c;
+    const I b = q / ((I)Wo * Ho);
+    const I s = ((b * H + 2 * ii) * W + 2 * j) * C + c;
     Vec8 a, t;
     a.load(x + s);
     t.load(x + s + C);
 #pragma unroll
     for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
-    t.load(x + s + (long)W * C);
+    t.load(x + s + (I)W * C);
 #pragma unroll
     for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
-    t.load(x + s + (long)W * C + C);
+    t.load(x + s + (I)W * C + C);
 #pragma unroll
     for (int k = 0; k < 8; k++) a.v[k] = 0.25f * (a.v[k] + t.v[k]);
     a.store(y + q * C + c);
@@ -354,14 +355,15 @@ __global__ void k_pool2(const bf16* __restrict__ x, bf16* __restrict__ y, int N,
 }
 
 // dx[n][y][x][c] = dy[n][y/2][x/2][c] / 4 (H, W: the pooling's input).
+template <class I>
 __global__ void k_pool2_bwd(const bf16* __restrict__ dy, bf16* __restrict__ dx, int N, int H, int W, int C) {
   const int G = C / 8;
-  const long n = (long)N * H * W * G;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  const I n = (I)N * H * W * G;
+  for (I i = blockIdx.x * (I)blockDim.x + threadIdx.x; i < n; i += (I)gridDim.x * blockDim.x) {
     const int c = (int)(i % G) * 8;
-    const long q = i / G;
+    const I q = i / G;
     const int xx = (int)(q % W), yy = (int)((q / W) % H);
-    const long b = q / ((long)W * H);
+    const I b = q / ((I)W * H);
     Vec8 a;
     a.load(dy + ((b * (H / 2) + yy / 2) * (W / 2) + xx / 2) * C + c);
 #pragma unroll
@@ -371,38 +373,40 @@ __global__ void k_pool2_bwd(const bf16* __restrict__ dy, bf16* __restrict__ dx, 
 }
 
 // y[n][y][x][c] = x[n][y/2][x/2][c] (H, W: the input's; the output is 2H x 2W).
+template <class I>
 __global__ void k_up2(const bf16* __restrict__ x, bf16* __restrict__ y, int N, int H, int W, int C) {
   const int Ho = 2 * H, Wo = 2 * W, G = C / 8;
-  const long n = (long)N * Ho * Wo * G;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  const I n = (I)N * Ho * Wo * G;
+  for (I i = blockIdx.x * (I)blockDim.x + threadIdx.x; i < n; i += (I)gridDim.x * blockDim.x) {
     const int c = (int)(i % G) * 8;
-    const long q = i / G;
+    const I q = i / G;
     const int xx = (int)(q % Wo), yy = (int)((q / Wo) % Ho);
-    const long b = q / ((long)Wo * Ho);
+    const I b = q / ((I)Wo * Ho);
     *reinterpret_cast<uint4*>(y + q * C + c) =
         *reinterpret_cast<const uint4*>(x + ((b * H + yy / 2) * W + xx / 2) * C + c);
   }
 }
 
 // dx[n][i][j][c] = sum of dy over the 2x2 block (H, W: the upsampling's input).
+template <class I>
 __global__ void k_up2_bwd(const bf16* __restrict__ dy, bf16* __restrict__ dx, int N, int H, int W, int C) {
   const int G = C / 8, Wo = 2 * W;
-  const long n = (long)N * H * W * G;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  const I n = (I)N * H * W * G;
+  for (I i = blockIdx.x * (I)blockDim.x + threadIdx.x; i < n; i += (I)gridDim.x * blockDim.x) {
     const int c = (int)(i % G) * 8;
-    const long q = i / G;
+    const I q = i / G;
     const int j = (int)(q % W), ii = (int)((q / W) % H);
-    const long b = q / ((long)W * H);
-    const long s = ((b * 2 * H + 2 * ii) * Wo + 2 * j) * C + c;
+    const I b = q / ((I)W * H);
+    const I s = ((b * 2 * H + 2 * ii) * Wo + 2 * j) * C + c;
     Vec8 a, t;
     a.load(dy + s);
     t.load(dy + s + C);
 #pragma unroll
     for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
-    t.load(dy + s + (long)Wo * C);
+    t.load(dy + s + (I)Wo * C);
 #pragma unroll
     for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
-    t.load(dy + s + (long)Wo * C + C);
+    t.load(dy + s + (I)Wo * C + C);
 #pragma unroll
     for (int k = 0; k < 8; k++) a.v[k] += t.v[k];
     a.store(dx + q * C + c);
@@ -540,21 +544,43 @@ cudaError_t nn_gelu_bwd(const void* pre, const void* dact, void* dpre, long n, c
   return cudaGetLastError();
 }
 
+// 32-bit index arithmetic (its divisions are several times cheaper than
+// 64-bit ones) whenever every element index fits.
+constexpr long kIndex32 = 0x7fffffffL;
+
 cudaError_t nn_pool2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s) {
   const long n = (long)N * H * W * C;
-  if (backward)
-    k_pool2_bwd<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
-  else
-    k_pool2<<<grid_for(n / 32), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
+  const bf16* in = static_cast<const bf16*>(x);
+  bf16* out = static_cast<bf16*>(y);
+  if (backward) {
+    if (4 * n <= kIndex32)
+      k_pool2_bwd<int><<<grid_for(n / 8), 256, 0, s>>>(in, out, N, H, W, C);
+    else
+      k_pool2_bwd<long><<<grid_for(n / 8), 256, 0, s>>>(in, out, N, H, W, C);
+  } else {
+    if (n <= kIndex32)
+      k_pool2<int><<<grid_for(n / 32), 256, 0, s>>>(in, out, N, H, W, C);
+    else
+      k_pool2<long><<<grid_for(n / 32), 256, 0, s>>>(in, out, N, H, W, C);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t nn_up2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s) {
   const long n = (long)N * H * W * C;
-  if (backward)
-    k_up2_bwd<<<grid_for(n / 8), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
-  else
-    k_up2<<<grid_for(n / 2), 256, 0, s>>>(static_cast<const bf16*>(x), static_cast<bf16*>(y), N, H, W, C);
+  const bf16* in = static_cast<const bf16*>(x);
+  bf16* out = static_cast<bf16*>(y);
+  if (backward) {
+    if (4 * n <= kIndex32)
+      k_up2_bwd<int><<<grid_for(n / 8), 256, 0, s>>>(in, out, N, H, W, C);
+    else
+      k_up2_bwd<long><<<grid_for(n / 8), 256, 0, s>>>(in, out, N, H, W, C);
+  } else {
+    if (4 * n <= kIndex32)
+      k_up2<int><<<grid_for(n / 2), 256, 0, s>>>(in, out, N, H, W, C);
+    else
+      k_up2<long><<<grid_for(n / 2), 256, 0, s>>>(in, out, N, H, W, C);
+  }
   return cudaGetLastError();
 }
 

@@ -3,7 +3,7 @@ statistically. Same seeded terrain (the 256^2 small config: fBm 1/64 +
 0.1 +- 0.02 sediment), wind normalize(1,0,1), 16,384 particles per cycle for
 10 cycles. The reference semantics run on the CPU oracle (bit-identical to
 the compiled reference) with three rand() seeds; their spread is the noise
-floor. Bounds: the GPU run (automatic lanes = max(1024, cells/64), a
+floor. Bounds: the GPU run (automatic lanes = max(1024, cells/256), a
 different random stream) must stay within 2.5x the noise floor in
 - W1: the 1-Wasserstein distance between the height histograms,
 - the RMS distance between the log10 radially averaged power spectra
