@@ -137,6 +137,10 @@ def _setup(L):
     L.swe_world_get_cycle.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64)]
     L.swe_world_set_cycle.argtypes = [_P, ctypes.c_uint64]
     L.swe_world_set_wait_limit.argtypes = [_P, ctypes.c_uint64]
+    L.swe_world_set_form.argtypes = [_P, ctypes.c_int, ctypes.c_int]
+    L.swe_world_get_form.argtypes = [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.swe_world_tune.argtypes = [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     L.swe_batch_erode.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.swe_batch_erode_ordered.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.swe_batch_create.argtypes = [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
@@ -381,6 +385,24 @@ class World:
     @cycle.setter
     def cycle(self, value: int) -> None:
         _check(lib.swe_world_set_cycle(self._h, ctypes.c_uint64(int(value))))
+
+    def set_form(self, kind: int, ctas: int = 0) -> None:
+        """Launch form of the PARALLEL kernel (0 default, 1 one cluster, 2 a
+        grid of `ctas` CTAs); changes no result."""
+        _check(lib.swe_world_set_form(self._h, int(kind), int(ctas)))
+
+    def form(self) -> tuple[int, int]:
+        k, c = ctypes.c_int(), ctypes.c_int()
+        _check(lib.swe_world_get_form(self._h, ctypes.byref(k), ctypes.byref(c)))
+        return k.value, c.value
+
+    def tune(self, particles: int) -> dict:
+        """swe_world_tune: the fastest launch form for `particles` per cycle,
+        timed on a scratch copy of this world and kept for it."""
+        k, c, b, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        _check(lib.swe_world_tune(self._h, int(particles), ctypes.byref(k), ctypes.byref(c), ctypes.byref(b),
+                                  ctypes.byref(d)))
+        return {"kind": k.value, "ctas": c.value, "best_ms": b.value, "default_ms": d.value}
 
     def set_wait_limit(self, ns: int) -> None:
         """Deadline (ns) of every wait inside a PARALLEL cycle; 0 restores

@@ -117,6 +117,7 @@ struct swe_world {
   // counts behind in maps that every cycle expects at zero; the next
   // parallel call clears them first.
   bool scratch_dirty = false;
+  swe::LaunchForm form;  // bounded-lanes launch form (default: the library's rule)
 
   Consts consts() const {
     Consts c;
@@ -224,9 +225,12 @@ int clear_after_abort(swe_world* w) {
 int enqueue_parallel_cycle(swe_world* w, int particles, int lanes) {
   SWE_CK(cudaMemsetAsync(w->gbar, 0, sizeof(swe::GridBarrier), w->stream));
   SWE_CK(swe::launch_par_cycle(w->pb, w->F, w->consts(), w->seed, w->cnt, w->gbar, particles, lanes,
-                               w->cycle_grid, w->stream));
+                               w->cycle_grid, w->stream, w->form));
   return SWE_OK;
 }
+
+std::mutex g_form_mutex;
+std::map<std::string, swe::LaunchForm> g_forms;  // (sides, particles, lanes) -> fastest form
 
 }  // namespace
 
@@ -448,6 +452,95 @@ int swe_world_set_wait_limit(swe_world* w, uint64_t ns) {
   if (!w) return fail(SWE_ERR_INVALID, "NULL world");
   w->wait_ns = ns;
   return SWE_OK;
+}
+
+int swe_world_set_form(swe_world* w, int kind, int ctas) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (kind < 0 || kind > 2 || ctas < 0) return fail(SWE_ERR_INVALID, "kind must be 0, 1 or 2 and ctas >= 0");
+  w->form.kind = kind;
+  w->form.ctas = ctas;
+  return SWE_OK;
+}
+
+int swe_world_get_form(swe_world* w, int* kind, int* ctas) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (kind) *kind = w->form.kind;
+  if (ctas) *ctas = w->form.ctas;
+  return SWE_OK;
+}
+
+int swe_world_tune(swe_world* w, int particles, int* kind, int* ctas, double* best_ms, double* default_ms) {
+  if (!w) return fail(SWE_ERR_INVALID, "NULL world");
+  if (particles < 1) return fail(SWE_ERR_INVALID, "particles must be >= 1");
+  if (int rc = use_device(w)) return rc;
+  const int lanes = swe::par_lanes(w->p.lanes, w->nx, w->nz, particles);
+  char key[96];
+  std::snprintf(key, sizeof key, "%dx%d:%d:%d", w->nx, w->nz, particles, lanes);
+  if (best_ms) *best_ms = 0.0;
+  if (default_ms) *default_ms = 0.0;
+  {
+    std::lock_guard<std::mutex> lock(g_form_mutex);
+    auto it = g_forms.find(key);
+    if (it != g_forms.end()) {
+      w->form = it->second;
+      if (kind) *kind = w->form.kind;
+      if (ctas) *ctas = w->form.ctas;
+      return SWE_OK;
+    }
+  }
+  // A scratch world with this world's size, parameters, seed and heights.
+  swe_world* r = nullptr;
+  if (int rc = swe_world_create(w->nx, w->nz, &w->p, w->seed, &r)) return rc;
+  int rc = SWE_OK;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto done = [&](int code) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    swe_world_destroy(r);
+    return code;
+  };
+  if (cudaMemcpyAsync(r->F.f[0], w->F.f[0], sizeof(float) * (size_t)w->n, cudaMemcpyDeviceToDevice, r->stream) !=
+          cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return done(fail(SWE_ERR_CUDA, "setting up the launch-form tuner failed"));
+  if ((rc = ensure_parallel(r, lanes)) != SWE_OK || (rc = ensure_fixed(r)) != SWE_OK) return done(rc);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, w->device);
+  std::vector<swe::LaunchForm> cands;
+  cands.push_back(swe::LaunchForm{0, 0});
+  cands.push_back(swe::LaunchForm{1, 0});
+  for (int div : {1, 2, 4}) cands.push_back(swe::LaunchForm{2, sms / div > 0 ? sms / div : 1});
+  cands.push_back(swe::LaunchForm{2, 3 * sms / 4 > 0 ? 3 * sms / 4 : 1});
+  double best = -1.0;
+  swe::LaunchForm best_form;
+  for (size_t i = 0; i <= cands.size(); i++) {
+    const swe::LaunchForm f = cands[i == 0 ? 0 : i - 1];  // the first form twice: a warm-up
+    r->form = f;
+    float ms = 0.0f;
+    if (cudaEventRecord(e0, r->stream) != cudaSuccess) return done(fail(SWE_ERR_CUDA, "event record failed"));
+    if ((rc = enqueue_parallel_cycle(r, particles, lanes)) != SWE_OK) return done(rc);
+    if (cudaEventRecord(e1, r->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      return done(fail(SWE_ERR_CUDA, "timing a launch form failed"));
+    if (i == 0) continue;
+    if (i == 1 && default_ms) *default_ms = ms;
+    if (best < 0 || ms < best) {
+      best = ms;
+      best_form = f;
+    }
+  }
+  uint32_t st = 0;
+  if ((rc = swe_world_status(r, &st)) != SWE_OK) return done(rc);
+  if (st) return done(fail(SWE_ERR_DEVICE, "a tuning cycle reported a device status"));
+  {
+    std::lock_guard<std::mutex> lock(g_form_mutex);
+    g_forms[key] = best_form;
+  }
+  w->form = best_form;
+  if (kind) *kind = best_form.kind;
+  if (ctas) *ctas = best_form.ctas;
+  if (best_ms) *best_ms = best;
+  return done(SWE_OK);
 }
 
 int swe_world_get_cycle(swe_world* w, uint64_t* cycle) {

@@ -72,9 +72,18 @@ void launch_height_to_fixed(const float* height, int32_t* q, const Consts& c, Co
 // Number of co-resident blocks of the persistent cycle kernel (0 if the
 // device cannot launch cooperative kernels).
 int cycle_grid(int device);
+// Launch form of a bounded-lanes cycle: kind 0 the default rule (one 16-CTA
+// cluster up to 4,096 lanes, else one CTA per SM), 1 one cluster (up to
+// 16,384 lanes), 2 a cooperative grid of `ctas` CTAs (0: one per SM). The
+// form changes no result: only the set of particles in flight matters.
+struct LaunchForm {
+  int kind = 0;
+  int ctas = 0;
+};
 // One parallel erode cycle as one cooperative kernel.
 cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
-                             Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s);
+                             Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s,
+                             const LaunchForm& form = LaunchForm());
 // Whether `lanes` particles in flight on an n-cell map take the bounded-lanes
 // kernel (one 16-CTA cluster, or one CTA per SM), whose particle state lives
 // in shared memory; otherwise launch_par_cycle needs B.state to hold them.

@@ -1726,7 +1726,8 @@ cudaError_t launch_lanes_grid(const CycleArgs& A, int ctas, int threads, int slo
 }  // namespace
 
 cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Consts& c, uint64_t seed,
-                             Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s) {
+                             Counters* cnt, GridBarrier* gb, int particles, int lanes, int grid, cudaStream_t s,
+                             const LaunchForm& form) {
   CycleArgs A;
   A.B = B;
   A.F = F;
@@ -1744,13 +1745,25 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms > 1024) sms = 1024;
   int threads = 0, slots = 0;
-  const bool cluster = lanes <= kClusterMaxLanes;
-  if (n <= (1l << 30) && lanes_shape(lanes, cluster ? kClusterCtas : sms,
+  // The form: by default one cluster up to kClusterMaxLanes lanes, else one
+  // CTA per SM; a requested form that cannot hold the lanes takes the default.
+  bool cluster = lanes <= kClusterMaxLanes;
+  int ctas = sms;
+  if (form.kind == 1 && lanes_shape(lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots)) {
+    cluster = true;
+  } else if (form.kind == 2) {
+    const int want = form.ctas > 0 && form.ctas < sms ? form.ctas : sms;
+    if (lanes_shape(lanes, want, kLanesGridMaxThreads, &threads, &slots)) {
+      cluster = false;
+      ctas = want;
+    }
+  }
+  if (n <= (1l << 30) && lanes_shape(lanes, cluster ? kClusterCtas : ctas,
                                      cluster ? kClusterMaxThreads : kLanesGridMaxThreads, &threads, &slots)) {
     k_cluster_prologue<<<sweep_grid(n), 256, 0, s>>>(B, n);
     bool launched = false;
     const cudaError_t e = cluster ? launch_cluster(A, threads, slots, s, &launched)
-                                  : launch_lanes_grid(A, sms, threads, slots, s, &launched);
+                                  : launch_lanes_grid(A, ctas, threads, slots, s, &launched);
     if (e != cudaSuccess) return e;
     if (launched) {
       k_ema_cycle<<<sweep_grid(n), 256, 0, s>>>(A);

@@ -143,3 +143,37 @@ def test_upload_download_roundtrip_every_field():
         assert np.array_equal(bits(w.download(f)), bits(a))
     with pytest.raises(swe.SweError):
         w.upload(swe.Field.HEIGHT, np.zeros(10, np.float32))
+
+
+@pytest.mark.parametrize("kind,ctas", [(1, 0), (2, 0), (2, 38), (2, 76), (2, 114)])
+def test_launch_forms_give_the_same_result(kind, ctas):
+    """Every launch form of the bounded-lanes kernel (one cluster, grids of
+    various CTA counts) leaves the world bit for bit as the CPU model does."""
+    port, w = _pair(96, 80, 7, WIND_101, 16, wseed=5, lanes=3000)
+    w.set_form(kind, ctas)
+    port.par_erode(12000, 2, seed=5)
+    w.erode(12000, 2, mode=swe.Mode.PARALLEL)
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), (kind, ctas, f)
+    w.close()
+
+
+def test_autotuner_leaves_the_world_alone_and_keeps_results():
+    port, w = _pair(128, 128, 3, WIND_101, 16, wseed=5, lanes=0)
+    before = [w.download(f).copy() for f in swe.FIELDS]
+    t = w.tune(16384)
+    assert t["best_ms"] > 0 and t["default_ms"] > 0 and t["best_ms"] <= t["default_ms"]
+    assert w.form() == (t["kind"], t["ctas"])
+    for f, b in zip(swe.FIELDS, before):
+        assert np.array_equal(bits(w.download(f)), bits(b)), f
+    assert w.cycle == 0
+    port.par_erode(16384, 1, seed=5)
+    w.erode(16384, 1, mode=swe.Mode.PARALLEL)
+    for f in swe.FIELDS:
+        assert np.array_equal(bits(port.get_field(int(f))), bits(w.download(f))), f
+    # cached: the same size, particles and lanes again
+    w2 = swe.World(128, params=swe.Params(pspeed=WIND_101, frac_bits=16), seed=5)
+    t2 = w2.tune(16384)
+    assert (t2["kind"], t2["ctas"]) == (t["kind"], t["ctas"]) and t2["best_ms"] == 0.0
+    w.close()
+    w2.close()
