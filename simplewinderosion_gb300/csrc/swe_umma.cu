@@ -6,22 +6,26 @@
 //   k_conv_tc   3x3 convolution, zero padding, NHWC bf16, as an implicit
 //               GEMM: rows = 128-pixel tiles of the output (two per CTA),
 //               columns = output channels, K = 9 taps x input channels.
-//               Per k-block (one tap, 8*KG input channels) the TMA loads the
-//               tap-shifted 128-pixel tile of the input straight from the
-//               NHWC tensor (pixels beyond the map edge arrive as zeros: the
-//               padding costs nothing), and a bulk copy brings the matching
-//               slice of the pre-packed weights. One thread issues the MMAs,
-//               one thread the copies; all four warps run the epilogue
-//               (TMEM -> registers, + bias, optional fused GELU, bf16 stores).
-//               The input gradient is the same kernel on the output gradient
-//               with the weights flipped and transposed at packing time.
-//
-// Shared-memory operands use the canonical K-major layout without swizzle:
-// 8x8 bf16 "core matrices" of 128 contiguous bytes, 8 rows of 16 bytes. A
-// TMA box of 8 channels x 128 pixels lands exactly as 16 such core matrices
-// stacked along M (the stride between them, SBO, is 128 bytes), and the next
-// 8 channels sit one box further on (LBO = 2048 bytes); the packed weights
-// are laid out the same way ([tap][channel group][n][8]).
+//               Per k-block (one tap, KC = 64, 32 or 16 input channels) the
+//               TMA loads the tap-shifted 128-pixel tile of the input
+//               straight from the NHWC tensor (pixels beyond the map edge
+//               arrive as zeros: the padding costs nothing) and the weight
+//               slice straight from the [n][tap][k] weights. One thread
+//               issues the copies, one the MMAs; all four warps run the
+//               epilogue (TMEM -> registers, + bias, optional fused GELU,
+//               bf16 stores). The input gradient is the same kernel on the
+//               output gradient with the weights flipped and transposed.
+//               Its operands sit in shared memory in the canonical K-major
+//               swizzled layout: one row of KC channels (128, 64 or 32
+//               bytes) per pixel or output channel, 8-row atoms SBO = 8 rows
+//               apart, the TMA writing the matching 128/64/32-byte swizzle;
+//               full rows keep every L2 sector access whole.
+//   k_wgrad_tc  the weight gradient: per tap a GEMM with M = output
+//               channels, N = input channels, K = pixels, both operands
+//               MN-major in the canonical layout without swizzle: a TMA box
+//               of 8 channels x 128 pixels is 16 core matrices (8 x 16 bytes)
+//               along K (LBO = 128 bytes), the next 8 channels one box
+//               further on (SBO = 2048 bytes).
 //
 // Every wait on an mbarrier is bounded (2 s by the global timer): past it the
 // kernel records an error code in g_tc_error, stops issuing work, waits
@@ -44,7 +48,6 @@ using bf16 = __nv_bfloat16;
 __device__ unsigned int g_tc_error;  // first failure code of a tensor-core kernel (0: none)
 
 constexpr int kTcThreads = 128;
-constexpr int kTcStages = 4;
 constexpr int kTcMTiles = 2;  // 128-pixel M tiles per CTA (they share each weight slice)
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
@@ -107,21 +110,30 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// Shared-memory matrix descriptor: start address, LBO (K direction), SBO
-// (M/N direction), descriptor version 1, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+// The same for a K-major operand in a swizzled layout (layout code `swz` in
+// bits 61-63: 2 = 128-byte, 4 = 64-byte, 6 = 32-byte swizzle): rows of one
+// swizzle span, 8-row atoms SBO bytes apart; LBO is not used (encoded 1).
+// Moving along K within a row adds the byte offset to the start address.
+__device__ __forceinline__ uint64_t smem_desc_sw(uint32_t addr, uint32_t sbo, uint32_t swz) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) |
+         ((uint64_t)swz << 61);
+}
+
+// General form: start address, LBO, SBO, layout code (0 = no swizzle).
+__device__ __forceinline__ uint64_t smem_desc_full(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t swz) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | ((uint64_t)swz << 61);
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
 }
 
 // Instruction descriptor of kind::f16: bf16 A and B, fp32 D, both K-major,
@@ -175,23 +187,27 @@ struct TcConvGeom {
   int kc;      // GEMM K channels (input channels of this convolution)
   int nc;      // GEMM N (output channels)
   int TW, R;   // an M tile: R image rows x TW pixels = 128 pixels
-  int KG;      // 8-channel groups per k-block
-  int chunks;  // kc / (8 KG)
+  int KC;      // channels per k-block: 64, 32 or 16, one swizzled row of 128, 64 or 32 bytes per pixel
+  int chunks;  // kc / KC
   int tiles;   // 128-pixel tiles in the batch
   int col_stride;  // TMEM columns between the CTA's M tiles
   int ncols;       // TMEM columns allocated
-  int stage_bytes, a_bytes;
+  int a_tile;      // bytes of one M tile's operand per k-block (128 rows)
+  int b_bytes;     // bytes of the weight slice per k-block (nc rows)
+  int stage_bytes;
+  int stages;       // pipeline depth (2..4)
+  uint32_t swz;    // descriptor layout code of the swizzle
 };
 
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_conv_tc(const __grid_constant__ CUtensorMap xmap, const bf16* __restrict__ wp, const float* __restrict__ bias,
-              bf16* __restrict__ y, bf16* __restrict__ act, const TcConvGeom g) {
+    k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap wmap,
+              const float* __restrict__ bias, bf16* __restrict__ y, bf16* __restrict__ act, const TcConvGeom g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTcStages * g.stage_bytes);
-  uint64_t* empty = full + kTcStages;
-  uint64_t* accum = empty + kTcStages;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + g.stages * g.stage_bytes);
+  uint64_t* empty = full + 4;
+  uint64_t* accum = empty + 4;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
   volatile int* consumed = abort + 1;  // k-blocks whose data the MMA thread took
@@ -202,7 +218,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int kblocks = 9 * g.chunks;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kTcStages; s++) {
+    for (int s = 0; s < g.stages; s++) {
       mbar_init(full + s, 1);
       mbar_init(empty + s, 1);
     }
@@ -224,7 +240,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   int issued = 0;  // producer: k-blocks whose copies were issued
   if (warp == 0 && lane == 0) {
-    // ---- producer: TMA for the shifted input tiles, bulk copy for the weights
+    // ---- producer: one TMA box per M tile for the tap-shifted input, one for the weight slice
     const int tiles_per_img = (g.H * g.W) >> 7;
     int tn[kTcMTiles], ty[kTcMTiles], tx[kTcMTiles];
 #pragma unroll
@@ -235,38 +251,36 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       ty[mt] = (q / (g.W / g.TW)) * g.R;
       tx[mt] = (q % (g.W / g.TW)) * g.TW;
     }
-    const uint32_t b_bytes = (uint32_t)g.KG * g.nc * 16;
-    const uint32_t bytes = (uint32_t)mt_n * g.KG * 2048 + b_bytes;
+    const uint32_t bytes = (uint32_t)mt_n * g.a_tile + g.b_bytes;
     for (int kb = 0; kb < kblocks; kb++) {
-      const int s = kb % kTcStages;
-      const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
+      const int s = kb % g.stages;
+      const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
       if (!mbar_wait(empty + s, ph ^ 1u, abort, true, 1u)) break;
       const int tap = kb / g.chunks, chunk = kb % g.chunks;
       const int dy = tap / 3 - 1, dx = tap % 3 - 1;
       unsigned char* st = smem + s * g.stage_bytes;
       mbar_expect_tx(full + s, bytes);
       for (int mt = 0; mt < mt_n; mt++)
-        for (int k = 0; k < g.KG; k++)
-          tma_load_4d(st + (mt * g.KG + k) * 2048, &xmap, full + s, (chunk * g.KG + k) * 8, tx[mt] + dx,
-                      ty[mt] + dy, tn[mt]);
-      bulk_load(st + g.a_bytes, wp + ((size_t)tap * g.kc + (size_t)chunk * g.KG * 8) * g.nc, b_bytes, full + s);
+        tma_load_4d(st + mt * g.a_tile, &xmap, full + s, chunk * g.KC, tx[mt] + dx, ty[mt] + dy, tn[mt]);
+      tma_load_3d(st + kTcMTiles * g.a_tile, &wmap, full + s, chunk * g.KC, tap, 0);
       issued = kb + 1;
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
     const uint32_t idesc = idesc_bf16(128, g.nc);
     const uint32_t sb = smem_u32(smem);
+    const uint32_t sbo = 16u * (uint32_t)g.KC;  // 8 rows of KC bf16
     int kb = 0;
     for (; kb < kblocks; kb++) {
-      const int s = kb % kTcStages;
-      const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
+      const int s = kb % g.stages;
+      const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
       if (!mbar_wait(full + s, ph, abort, true, 2u)) break;
       tc_fence_after();
-      const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + g.a_bytes;
+      const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + kTcMTiles * g.a_tile;
       for (int mt = 0; mt < mt_n; mt++) {
-        for (int j = 0; j < g.KG / 2; j++) {
-          const uint64_t ad = smem_desc(a0 + (mt * g.KG + 2 * j) * 2048, 2048, 128);
-          const uint64_t bd = smem_desc(b0 + 2 * j * g.nc * 16, g.nc * 16, 128);
+        for (int j = 0; j < g.KC / 16; j++) {
+          const uint64_t ad = smem_desc_sw(a0 + mt * g.a_tile + 32 * j, sbo, g.swz);
+          const uint64_t bd = smem_desc_sw(b0 + 32 * j, sbo, g.swz);
           umma_bf16(tmem + mt * g.col_stride, ad, bd, idesc, (kb > 0 || j > 0) ? 1u : 0u);
         }
       }
@@ -323,7 +337,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();  // the MMA thread's count of consumed k-blocks is visible
   if (warp == 0 && lane == 0) {
     for (int kb = *consumed; kb < issued; kb++)
-      mbar_wait(full + kb % kTcStages, (uint32_t)(kb / kTcStages) & 1u, abort, false, 4u);
+      mbar_wait(full + kb % g.stages, (uint32_t)(kb / g.stages) & 1u, abort, false, 4u);
   }
   tc_fence_before();
   __syncthreads();
@@ -332,7 +346,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 struct TcWgradGeom {
   int H, W, cin, cout;
-  int TW, R;          // an M tile: R image rows x TW pixels = 128 pixels
+  int TW, R;          // a pixel tile: R image rows x TW pixels = 128 pixels
+  int cw, cr;         // a 16-pixel chunk of the tile: cr rows x cw pixels
+  int MA, MB;         // channels per swizzled row of dy (A) and of x (B): 64, 32 or 16
+  uint32_t swzA, swzB;
   int tiles;          // 128-pixel tiles in the batch
   int tiles_per_cta;  // the CTA's share of the pixel sum (split K)
   int taps;           // taps per CTA (9, or 3: one row of taps per blockIdx.y)
@@ -340,27 +357,26 @@ struct TcWgradGeom {
   int ncols;
   int stages;
   int a_bytes, stage_bytes;
-  int tail;  // bytes after the stages: the 128 padded M rows of the last stage's A stay in the allocation
+  int tail;  // bytes after the stages, so that the padded M rows of the last A operand stay in the allocation
 };
 
 // Weight gradient dW[co][tap][ci] += sum over pixels p of dy[p][co] x[p + tap][ci]
 // as a GEMM per tap with M = output channels (padded to 128; the rows past
 // cout are never stored), N = input channels, K = pixels, split over CTAs by
 // pixel tiles and over blockIdx.y by rows of taps. Both operands are
-// MN-major in shared memory (channels contiguous): a TMA box of 8 channels x
-// 128 pixels is 16 core matrices along K (LBO = 128 bytes) and the next 8
-// channels sit one box further on (SBO = 2048 bytes). Per k-block (one pixel
-// tile, one tap) the TMA brings the dy tile and the tap-shifted x tile
-// (zeros past the map edge). The partial sums leave TMEM through fp32
-// atomics into dw.
+// MN-major (channels contiguous) in the canonical swizzled layout: for each
+// 16-pixel K step, a TMA box of MA (or MB) channels x 16 pixels is 16 rows of
+// MA*2 bytes (8-row atoms SBO = 16*MA bytes apart along K), the next MA
+// channels one box further on (LBO = 32*MA bytes along M or N). Per k-block
+// (one 128-pixel tile, one tap) the TMA brings the dy tile and the
+// tap-shifted x tile (zeros past the map edge). The partial sums leave TMEM
+// through fp32 atomics into dw.
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap,
                float* __restrict__ dw, const TcWgradGeom g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  // stages, then a tail that keeps the padded M rows of the last stage's A
-  // operand inside the allocation, then the barriers
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + g.stages * g.stage_bytes + g.tail);
   uint64_t* empty = full + 4;
   uint64_t* accum = empty + 4;
@@ -398,7 +414,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   int issued = 0;
   if (warp == 0 && lane == 0) {
     const int tiles_per_img = (g.H * g.W) >> 7;
-    const uint32_t bytes = (uint32_t)(g.cout / 8 + g.cin / 8) * 2048;
+    const uint32_t bytes = 256u * (uint32_t)(g.cout + g.cin);  // 8 K steps x 16 pixels x channels x 2 bytes
     for (int kb = 0; kb < kblocks; kb++) {
       const int s = kb % g.stages;
       const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
@@ -409,9 +425,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const int dy = tap / 3 - 1, dx = tap % 3 - 1;
       unsigned char* st = smem + s * g.stage_bytes;
       mbar_expect_tx(full + s, bytes);
-      for (int k = 0; k < g.cout / 8; k++) tma_load_4d(st + k * 2048, &dymap, full + s, 8 * k, tx, ty, tn);
-      for (int k = 0; k < g.cin / 8; k++)
-        tma_load_4d(st + g.a_bytes + k * 2048, &xmap, full + s, 8 * k, tx + dx, ty + dy, tn);
+      for (int k16 = 0; k16 < 8; k16++) {
+        // tile pixels 16 k16 .. 16 k16 + 15: cr rows of cw pixels
+        const int cx = tx + (16 * k16) % g.TW, cy = ty + (16 * k16) / g.TW;
+        unsigned char* a = st + k16 * 32 * g.cout;
+        unsigned char* b = st + g.a_bytes + k16 * 32 * g.cin;
+        for (int m = 0; m < g.cout / g.MA; m++) tma_load_4d(a + m * 32 * g.MA, &dymap, full + s, m * g.MA, cx, cy, tn);
+        for (int m = 0; m < g.cin / g.MB; m++)
+          tma_load_4d(b + m * 32 * g.MB, &xmap, full + s, m * g.MB, cx + dx, cy + dy, tn);
+      }
       issued = kb + 1;
     }
   } else if (warp == 1 && lane == 0) {
@@ -427,8 +449,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + g.a_bytes;
 #pragma unroll
       for (int k16 = 0; k16 < 8; k16++) {
-        const uint64_t ad = smem_desc(a0 + 256 * k16, 128, 2048);
-        const uint64_t bd = smem_desc(b0 + 256 * k16, 128, 2048);
+        const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.cout, 32 * g.MA, 16 * g.MA, g.swzA);
+        const uint64_t bd = smem_desc_full(b0 + k16 * 32 * g.cin, 32 * g.MB, 16 * g.MB, g.swzB);
         umma_bf16(tmem + j * g.col_stride, ad, bd, idesc, (i > 0 || k16 > 0) ? 1u : 0u);
       }
       umma_commit(empty + s);
@@ -465,24 +487,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.ncols) : "memory");
 }
 
-// Packed weights of a convolution for k_conv_tc: wp[tap][k/8][n][k%8] with
-// K the convolution's input channels and N its output channels. Forward:
-// w[n][tap][k] (w bf16 [cout][3][3][cin]). Input gradient (flip): the
-// convolution of dy with the flipped, transposed weights, K = cout, N = cin:
-// w[k][8 - tap][n].
-__global__ void k_pack_tc(const bf16* __restrict__ w, bf16* __restrict__ wp, int cin, int cout, int flip) {
-  const int kc = flip ? cout : cin, nc = flip ? cin : cout;
-  const long total = 9l * kc * nc;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int tap = (int)(i / ((long)kc * nc));
-    const int rem = (int)(i % ((long)kc * nc));
-    const int gk = rem / (nc * 8);
-    const int r2 = rem % (nc * 8);
-    const int n = r2 >> 3, k = gk * 8 + (r2 & 7);
-    wp[i] = flip ? w[((long)k * 9 + (8 - tap)) * cin + n] : w[((long)n * 9 + tap) * cin + k];
-  }
-}
-
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -515,11 +519,32 @@ bool nn_conv_tc_supported(int H, int W, int kc, int nc) {
 }
 
 cudaError_t nn_pack_tc(const void* w, void* wp, int cin, int cout, bool flip, cudaStream_t s) {
-  const long total = 9l * cin * cout;
-  const int grid = (int)((total + 255) / 256 < 1024 ? (total + 255) / 256 : 1024);
-  k_pack_tc<<<grid, 256, 0, s>>>(static_cast<const bf16*>(w), static_cast<bf16*>(wp), cin, cout, flip ? 1 : 0);
-  return cudaGetLastError();
+  // The kernel reads weights as [n][tap][k] through a tensor map: the
+  // forward weights as they are ([cout][3][3][cin]), the input gradient's
+  // flipped and transposed ([cin][3][3][cout], tap -> 8 - tap).
+  if (flip) return nn_flip(w, wp, cin, cout, s);
+  return cudaMemcpyAsync(wp, w, sizeof(bf16) * 9 * (size_t)cin * cout, cudaMemcpyDeviceToDevice, s);
 }
+
+namespace {
+
+// A bf16 tensor map over `rank` dims (innermost first) with the given box and
+// the swizzle that matches a box row of `row_bytes` (128, 64 or 32).
+cudaError_t make_map(CUtensorMap* map, const void* t, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
+                     const cuuint32_t* box, int row_bytes) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  const CUtensorMapSwizzle sw = row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                  : CU_TENSOR_MAP_SWIZZLE_32B;
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(t), dims, strides,
+                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace
 
 cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y, void* act, int N, int H, int W,
                        int kc, int nc, cudaStream_t s) {
@@ -527,8 +552,6 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   if ((reinterpret_cast<uintptr_t>(x) & 15) || (reinterpret_cast<uintptr_t>(wp) & 15) ||
       (reinterpret_cast<uintptr_t>(y) & 15) || (act && (reinterpret_cast<uintptr_t>(act) & 15)))
     return cudaErrorMisalignedAddress;
-  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
-  if (!enc) return cudaErrorNotSupported;
   TcConvGeom g;
   g.H = H;
   g.W = W;
@@ -536,52 +559,39 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   g.nc = nc;
   g.TW = tile_width(W);
   g.R = 128 / g.TW;
-  g.KG = (kc / 8) % 4 == 0 ? 4 : 2;
-  g.chunks = kc / (8 * g.KG);
+  g.KC = kc % 64 == 0 ? 64 : (kc % 32 == 0 ? 32 : 16);
+  g.chunks = kc / g.KC;
   const long pixels = (long)N * H * W;
   g.tiles = (int)(pixels / 128);
   g.col_stride = (nc + 31) / 32 * 32;
   int cols = 32;
   while (cols < kTcMTiles * g.col_stride) cols <<= 1;
   g.ncols = cols;
-  g.a_bytes = kTcMTiles * g.KG * 2048;
-  g.stage_bytes = (g.a_bytes + g.KG * nc * 16 + 1023) / 1024 * 1024;
-  const size_t smem = 1024 + (size_t)kTcStages * g.stage_bytes + (2 * kTcStages + 1) * 8 + 16;
+  g.a_tile = 128 * g.KC * 2;
+  g.b_bytes = nc * g.KC * 2;
+  g.stage_bytes = (kTcMTiles * g.a_tile + g.b_bytes + 1023) / 1024 * 1024;
+  g.swz = g.KC == 64 ? 2u : (g.KC == 32 ? 4u : 6u);
+  g.stages = 4;
+  while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + 128 > 220 * 1024) g.stages--;
+  const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + 128;
+  if (smem > 227 * 1024) return cudaErrorNotSupported;
 
-  CUtensorMap map;
-  const cuuint64_t dims[4] = {(cuuint64_t)kc, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
-  const cuuint64_t strides[3] = {(cuuint64_t)kc * 2, (cuuint64_t)W * kc * 2, (cuuint64_t)H * W * kc * 2};
-  const cuuint32_t box[4] = {8, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  CUtensorMap xm, wm;
+  const cuuint64_t xd[4] = {(cuuint64_t)kc, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t xs[3] = {(cuuint64_t)kc * 2, (cuuint64_t)W * kc * 2, (cuuint64_t)H * W * kc * 2};
+  const cuuint32_t xb[4] = {(cuuint32_t)g.KC, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
+  const cuuint64_t wd[3] = {(cuuint64_t)kc, 9, (cuuint64_t)nc};
+  const cuuint64_t ws[2] = {(cuuint64_t)kc * 2, (cuuint64_t)9 * kc * 2};
+  const cuuint32_t wb[3] = {(cuuint32_t)g.KC, 1, (cuuint32_t)nc};
+  cudaError_t e = make_map(&xm, x, 4, xd, xs, xb, g.KC * 2);
+  if (e == cudaSuccess) e = make_map(&wm, wp, 3, wd, ws, wb, g.KC * 2);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int grid = (g.tiles + kTcMTiles - 1) / kTcMTiles;
-  k_conv_tc<<<grid, kTcThreads, smem, s>>>(map, static_cast<const bf16*>(wp), bias, static_cast<bf16*>(y),
-                                           static_cast<bf16*>(act), g);
+  k_conv_tc<<<grid, kTcThreads, smem, s>>>(xm, wm, bias, static_cast<bf16*>(y), static_cast<bf16*>(act), g);
   return cudaGetLastError();
 }
-
-namespace {
-
-// NHWC bf16 tensor map with boxes of 8 channels x (TW pixels x R rows).
-cudaError_t nhwc_map(CUtensorMap* map, const void* t, int N, int H, int W, int C, int TW, int R) {
-  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
-  if (!enc) return cudaErrorNotSupported;
-  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
-  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-  const cuuint32_t box[4] = {8, (cuuint32_t)TW, (cuuint32_t)R, 1};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(t), dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
-
-}  // namespace
 
 bool nn_wgrad_tc_supported(int H, int W, int cin, int cout) {
   return nn_conv_tc_supported(H, W, cin, cin) && cout >= 16 && cout % 16 == 0 && cout <= 128 && cin <= 128;
@@ -598,16 +608,22 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   g.cout = cout;
   g.TW = tile_width(W);
   g.R = 128 / g.TW;
+  g.cw = g.TW < 16 ? g.TW : 16;
+  g.cr = 16 / g.cw;
+  g.MA = cout % 64 == 0 ? 64 : (cout % 32 == 0 ? 32 : 16);
+  g.MB = cin % 64 == 0 ? 64 : (cin % 32 == 0 ? 32 : 16);
+  g.swzA = g.MA == 64 ? 2u : (g.MA == 32 ? 4u : 6u);
+  g.swzB = g.MB == 64 ? 2u : (g.MB == 32 ? 4u : 6u);
   g.tiles = (int)((long)N * H * W / 128);
   g.col_stride = (cin + 31) / 32 * 32;
   g.taps = 9 * g.col_stride <= 512 ? 9 : 3;
   int cols = 32;
   while (cols < g.taps * g.col_stride) cols <<= 1;
   g.ncols = cols;
-  g.a_bytes = cout / 8 * 2048;
-  g.stage_bytes = g.a_bytes + cin / 8 * 2048;
-  // the MMA reads 128 rows of A (16 channel groups x 2048 bytes) from each stage
-  g.tail = g.stage_bytes < 32768 ? 32768 - g.stage_bytes : 0;
+  g.a_bytes = 256 * cout;  // 8 K steps x 16 pixels x cout x 2 bytes
+  g.stage_bytes = g.a_bytes + 256 * cin;
+  // the MMA reads 128 rows of A from the last K step: up to 4 KiB past its start
+  g.tail = 4096;
   g.stages = 4;
   while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128 > 200 * 1024) g.stages--;
   const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;
@@ -619,8 +635,14 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   g.tiles_per_cta = (g.tiles + ctas_x - 1) / ctas_x;
   ctas_x = (g.tiles + g.tiles_per_cta - 1) / g.tiles_per_cta;
   CUtensorMap xm, dm;
-  cudaError_t e = nhwc_map(&xm, x, N, H, W, cin, g.TW, g.R);
-  if (e == cudaSuccess) e = nhwc_map(&dm, dy, N, H, W, cout, g.TW, g.R);
+  const cuuint64_t xd[4] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t xs[3] = {(cuuint64_t)cin * 2, (cuuint64_t)W * cin * 2, (cuuint64_t)H * W * cin * 2};
+  const cuuint32_t xb[4] = {(cuuint32_t)g.MB, (cuuint32_t)g.cw, (cuuint32_t)g.cr, 1};
+  const cuuint64_t dd[4] = {(cuuint64_t)cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+  const cuuint64_t ds[3] = {(cuuint64_t)cout * 2, (cuuint64_t)W * cout * 2, (cuuint64_t)H * W * cout * 2};
+  const cuuint32_t db[4] = {(cuuint32_t)g.MA, (cuuint32_t)g.cw, (cuuint32_t)g.cr, 1};
+  cudaError_t e = make_map(&xm, x, 4, xd, xs, xb, g.MB * 2);
+  if (e == cudaSuccess) e = make_map(&dm, dy, 4, dd, ds, db, g.MA * 2);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
