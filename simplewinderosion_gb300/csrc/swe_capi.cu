@@ -511,6 +511,7 @@ int swe_world_tune(swe_world* w, int particles, int* kind, int* ctas, double* be
   cands.push_back(swe::LaunchForm{1, 0});
   for (int div : {1, 2, 4}) cands.push_back(swe::LaunchForm{2, sms / div > 0 ? sms / div : 1});
   cands.push_back(swe::LaunchForm{2, 3 * sms / 4 > 0 ? 3 * sms / 4 : 1});
+  cands.push_back(swe::LaunchForm{2, 2 * sms});  // two CTAs per SM, where they fit
   double best = -1.0;
   swe::LaunchForm best_form;
   for (size_t i = 0; i <= cands.size(); i++) {

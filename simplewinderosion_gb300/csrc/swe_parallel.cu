@@ -1704,6 +1704,13 @@ cudaError_t launch_cluster(const CycleArgs& A, int threads, int slots, cudaStrea
   return e;
 }
 
+int sms_of_current() {
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
 cudaError_t launch_lanes_grid(const CycleArgs& A, int ctas, int threads, int slots, cudaStream_t s,
                               bool* launched) {
   *launched = false;
@@ -1712,9 +1719,9 @@ cudaError_t launch_lanes_grid(const CycleArgs& A, int ctas, int threads, int slo
   int per_sm = 0;
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_par_lanes<false>, threads, smem);
-  if (e != cudaSuccess || per_sm < 1) {
+  if (e != cudaSuccess || per_sm < 1 || ctas > per_sm * sms_of_current()) {
     cudaGetLastError();
-    return cudaSuccess;
+    return cudaSuccess;  // not co-resident: the caller takes another form
   }
   int sl = slots;
   void* args[] = {const_cast<CycleArgs*>(&A), &sl};
@@ -1752,7 +1759,7 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   if (form.kind == 1 && lanes_shape(lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots)) {
     cluster = true;
   } else if (form.kind == 2) {
-    const int want = form.ctas > 0 && form.ctas < sms ? form.ctas : sms;
+    const int want = form.ctas > 0 && form.ctas <= 2 * sms ? form.ctas : sms;
     if (lanes_shape(lanes, want, kLanesGridMaxThreads, &threads, &slots)) {
       cluster = false;
       ctas = want;
