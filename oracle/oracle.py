@@ -263,6 +263,8 @@ class Reference:
             L.ref_trace.argtypes = [ctypes.c_int, _P, _P, ctypes.c_int, _P, _P]
             L.ref_fly_live.argtypes = [ctypes.c_float, ctypes.c_float, _P, ctypes.c_int, _P, _P]
             L.ref_probe_order.argtypes = [_P]
+            L.ref_map_init.argtypes = [ctypes.c_int]
+            L.ref_updatenode.argtypes = [_P]
             Reference._libs[n] = L
         self.L = Reference._libs[n]
         self.nx = self.nz = n
@@ -329,6 +331,17 @@ class Reference:
         ok = self.L.ref_fly_live(ctypes.c_float(x), ctypes.c_float(z), _ptr(ps), steps,
                                  _ptr(tp) if tp is not None else None, _ptr(out))
         return out, ok
+
+    def map_init(self, seed: int = 0) -> np.ndarray:
+        """quad::map::init's own terrain (the bump), returned as heights."""
+        self.L.ref_map_init(seed)
+        return self.get_field(0)
+
+    def vertices(self) -> np.ndarray:
+        """updatenode's vertex data per cell: [n, n, 12] (P, N, T-P, B-P)."""
+        out = np.zeros(self.n * 12, dtype=np.float32)
+        self.L.ref_updatenode(_ptr(out))
+        return out.reshape(self.nx, self.nz, 12)
 
     def probe_order(self):
         o = np.empty(7, dtype=np.int32)

@@ -97,6 +97,35 @@ extern "C" {
 
 int ref_size(void) { return quad::size; }
 
+// quad::map::init (cellpool.h:339-430) itself, on a fresh cell pool: the
+// node set-up, indexnode, then the reference's own terrain (the Gaussian bump
+// normalised to [0, 0.5]); the other fields are zeroed afterwards as in
+// ensure_init (new cell[] leaves them uninitialised, cellpool.h:141). Its
+// progress lines go to stdout.
+void ref_map_init(int seed) {
+  static Vertexpool<Vertex> vp;
+  static mappool::pool<quad::cell> pool;
+  pool.reserve(quad::area);
+  World::map.init(vp, pool, seed);
+  quad::cell* c = World::map.nodes[0].s.root.start;
+  for (int i = 0; i < quad::area; i++) {
+    const float h = c[i].height;
+    std::memset(&c[i], 0, sizeof(quad::cell));
+    c[i].height = h;
+  }
+  g_ready = true;
+}
+
+// updatenode (cellpool.h:302-333) over the current map: 12 floats per cell
+// (P, normal, T - P, B - P) into out, at index math::flatten(pos).
+void ref_updatenode(float* out) {
+  ensure_init();
+  static Vertexpool<Vertex> vp;
+  vp.capture = out;
+  updatenode(vp, World::map.nodes[0]);
+  vp.capture = nullptr;
+}
+
 void ref_set_field(int f, const float* src) {
   ensure_init();
   quad::cell* c = cells();

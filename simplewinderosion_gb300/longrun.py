@@ -67,6 +67,8 @@ def long_run(model: Surrogate, size: int = 4096, jumps: int = 8, judge_every: in
     plain = World(size, params=params, seed=seed * 1000 + 1)
     plain.terrain(**t)
     particles = size * size
+    acc.tune(particles)  # the fastest launch form for this size (timed on a scratch copy)
+    plain.tune(particles)
     rec = {"size": size, "jumps": jumps, "judge_every": judge_every, "tile": tile, "halo": halo,
            "particles_per_cycle": particles, "jump_cycles": JUMP_CYCLES, "steps": []}
     t_sur = t_judge = t_plain = 0.0

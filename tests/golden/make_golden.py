@@ -8,7 +8,7 @@ stored as .npz so machines without the reference sources (the GPU machine) can
 check the oracle port and the CUDA kernels against the reference's own
 results.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [--only-new]
 """
 from __future__ import annotations
 
@@ -115,6 +115,26 @@ def trace_case(name, n, seed, count, steps, pspeed):
                         pspeed=np.asarray(pspeed, np.float32))
 
 
+def map_init_case(name, n):
+    """quad::map::init's own terrain (the Gaussian bump normalised to [0, 0.5],
+    cellpool.h:339-430), from the compiled reference."""
+    ref = oracle.Reference(n)
+    np.savez_compressed(OUT / f"{name}.npz", height=ref.map_init(0), n=n)
+
+
+def vertices_case(name, n, seed):
+    """updatenode's vertex data (cellpool.h:302-333: position, normal, +x and
+    +z edges per cell) on a map with random heights, a flat patch and a
+    cliff, captured from the compiled reference's own updatenode."""
+    ref = oracle.Reference(n)
+    rs = np.random.RandomState(seed)
+    h = rs.uniform(0, 0.5, size=(n, n)).astype(np.float32)
+    h[: n // 3, : n // 3] = 0.25
+    h[n // 2:, :] += 0.3
+    ref.reset(h)
+    np.savez_compressed(OUT / f"{name}.npz", height=h, vertices=ref.vertices())
+
+
 def rand_case(name):
     ref = oracle.Reference(8)
     seeds = [0, 1, 7, 12345, 2**31 + 5, 4294967295]
@@ -128,8 +148,12 @@ def rand_case(name):
                         order=ref.probe_order())
 
 
-def main():
+def main(argv):
     oracle.build_reference(sizes=(8, 16, 32, 48, 64))
+    map_init_case("map_init_48", 48)
+    vertices_case("vertices_16", 16, 31)
+    if "--only-new" in argv:
+        return
     rand_case("rand_sequences")
     erode_case("erode_32_default", 32, 11, 5, 40, 4)
     erode_case("erode_64_wind101", 64, 12, 99, 120, 3, pspeed=WIND_101)
@@ -144,4 +168,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

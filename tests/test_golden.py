@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
+from simplewinderosion_gb300 import terrain
 from tests.conftest import bits, golden
 
 X86 = platform.machine() in ("x86_64", "AMD64")
@@ -85,3 +86,31 @@ def test_golden_trace(name):
     port.set_field(0, g["height"])
     got = port.trace(g["spawn"], rec.shape[1], trace_tape(int(g["tape_seed"]), rec.shape[0], rec.shape[1]))
     _check(rec, got, atol=1e-4)
+
+
+def test_reference_bump_restatement_is_the_compiled_map_init():
+    """terrain.reference_bump restates quad::map::init's terrain
+    (cellpool.h:380-428): bit for bit what the compiled reference built."""
+    g = golden("map_init_48")
+    n = int(g["n"])
+    assert np.array_equal(bits(terrain.reference_bump(n)), bits(g["height"]))
+
+
+def test_vertex_restatement_is_the_compiled_updatenode():
+    """The vertex layout the library's swe_world_vertices writes (position,
+    normal, +x edge, +z edge per cell; edges to cells past the map read height
+    0) against the compiled reference's own updatenode (cellpool.h:302-333),
+    with the normals from the reference's quad::_normal."""
+    g = golden("vertices_16")
+    h, v = g["height"], g["vertices"]
+    n = h.shape[0]
+    m = np.float32(80.0)
+    hp = np.zeros((n + 1, n + 1), np.float32)
+    hp[:n, :n] = h
+    py = (m * h).astype(np.float32)
+    assert np.array_equal(v[..., 0], np.broadcast_to(np.arange(n, dtype=np.float32)[:, None], (n, n)))
+    assert np.array_equal(bits(v[..., 1]), bits(py))
+    assert np.array_equal(bits(v[..., 7]), bits((m * hp[1:, :n]).astype(np.float32) - py))
+    assert np.array_equal(bits(v[..., 10]), bits((m * hp[:n, 1:]).astype(np.float32) - py))
+    assert np.all(v[..., 6] == 1.0) and np.all(v[..., 11] == 1.0)
+    assert np.all(v[..., 8] == 0.0) and np.all(v[..., 9] == 0.0)

@@ -70,3 +70,29 @@ def test_vertices_are_updatenode():
     assert v.shape == (48, 40, 12)
     assert np.array_equal(v.view(np.int32), want.view(np.int32))
     w.close()
+
+
+def test_vertices_equal_the_compiled_updatenode():
+    """swe_world_vertices bit for bit the compiled reference's own updatenode
+    output (tests/golden/vertices_16.npz: positions, normals and edges)."""
+    from tests.conftest import golden
+    g = golden("vertices_16")
+    n = g["height"].shape[0]
+    w = swe.World(n, seed=1)
+    w.upload(swe.Field.HEIGHT, g["height"])
+    assert np.array_equal(w.vertices().view(np.int32), np.asarray(g["vertices"], np.float32).view(np.int32))
+    w.close()
+
+
+def test_device_bump_equals_the_compiled_map_init():
+    """swe_world_terrain's octaves-0 terrain against the compiled reference's
+    quad::map::init (tests/golden/map_init_48.npz): within one float ulp (the
+    device rounds exp(double) its own way)."""
+    from tests.conftest import golden
+    g = golden("map_init_48")
+    n = int(g["n"])
+    w = swe.World(n, seed=1)
+    w.terrain()
+    d = np.abs(w.height.view(np.int32).astype(np.int64) - np.asarray(g["height"], np.float32).view(np.int32))
+    assert d.max() <= 1, d.max()
+    w.close()
