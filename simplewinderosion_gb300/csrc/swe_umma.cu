@@ -190,31 +190,43 @@ struct TcConvGeom {
   int KC;      // channels per k-block: 64, 32 or 16, one swizzled row of 128, 64 or 32 bytes per pixel
   int chunks;  // kc / KC
   int tiles;   // 128-pixel tiles in the batch
-  int col_stride;  // TMEM columns between the CTA's M tiles
+  int pairs;   // units of work: kTcMTiles consecutive tiles that share every weight slice
+  int col_stride;  // TMEM columns between the M tiles of a unit
+  int nbuf;        // TMEM accumulator sets (2: the epilogue of one unit overlaps the next unit's MMAs)
   int ncols;       // TMEM columns allocated
   int a_tile;      // bytes of one M tile's operand per k-block (128 rows)
   int b_bytes;     // bytes of the weight slice per k-block (nc rows)
   int stage_bytes;
-  int stages;       // pipeline depth (2..4)
+  int stages;      // pipeline depth (2..6)
   uint32_t swz;    // descriptor layout code of the swizzle
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+constexpr int kConvWarps = 6;  // warp 0 copies, warp 1 issues the MMAs, warps 2-5 run the epilogue
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent: each CTA takes units (pairs of M tiles) blockIdx.x,
+// blockIdx.x + gridDim.x, ...; the copies and MMAs run ahead through the
+// units' k-blocks in one stage ring while the epilogue warps drain the
+// previous unit's accumulators from the other TMEM set.
+__global__ void __launch_bounds__(kConvWarps * 32, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap wmap,
               const float* __restrict__ bias, bf16* __restrict__ y, bf16* __restrict__ act, const TcConvGeom g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + g.stages * g.stage_bytes);
-  uint64_t* empty = full + 4;
-  uint64_t* accum = empty + 4;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* empty = full + 8;
+  uint64_t* tfull = empty + 8;   // accumulator set b holds a finished unit
+  uint64_t* tempty = tfull + 2;  // accumulator set b was drained by the epilogue
+  uint64_t* drain = tempty + 2;  // every MMA this CTA issued has completed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
   volatile int* consumed = abort + 1;  // k-blocks whose data the MMA thread took
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile0 = blockIdx.x * kTcMTiles;
-  const int mt_n = min(kTcMTiles, g.tiles - tile0);
   const int kblocks = 9 * g.chunks;
 
   if (threadIdx.x == 0) {
@@ -222,7 +234,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(full + s, 1);
       mbar_init(empty + s, 1);
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(tfull + b, 1);
+      mbar_init(tempty + b, 4);
+    }
+    mbar_init(drain, 1);
     *abort = 0;
     *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -237,99 +253,130 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const int tiles_per_img = (g.H * g.W) >> 7;
 
   int issued = 0;  // producer: k-blocks whose copies were issued
-  if (warp == 0 && lane == 0) {
-    // ---- producer: one TMA box per M tile for the tap-shifted input, one for the weight slice
-    const int tiles_per_img = (g.H * g.W) >> 7;
-    int tn[kTcMTiles], ty[kTcMTiles], tx[kTcMTiles];
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- producer: one TMA box per M tile for the tap-shifted input, one for the weight slice
+      int kbg = 0;
+      for (int u = blockIdx.x; u < g.pairs && !*abort; u += gridDim.x) {
+        const int tile0 = u * kTcMTiles, mt_n = min(kTcMTiles, g.tiles - tile0);
+        int tn[kTcMTiles], ty[kTcMTiles], tx[kTcMTiles];
 #pragma unroll
-    for (int mt = 0; mt < kTcMTiles; mt++) {
-      const int t = tile0 + mt;
-      const int q = t % tiles_per_img;
-      tn[mt] = t / tiles_per_img;
-      ty[mt] = (q / (g.W / g.TW)) * g.R;
-      tx[mt] = (q % (g.W / g.TW)) * g.TW;
-    }
-    const uint32_t bytes = (uint32_t)mt_n * g.a_tile + g.b_bytes;
-    for (int kb = 0; kb < kblocks; kb++) {
-      const int s = kb % g.stages;
-      const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
-      if (!mbar_wait(empty + s, ph ^ 1u, abort, true, 1u)) break;
-      const int tap = kb / g.chunks, chunk = kb % g.chunks;
-      const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-      unsigned char* st = smem + s * g.stage_bytes;
-      mbar_expect_tx(full + s, bytes);
-      for (int mt = 0; mt < mt_n; mt++)
-        tma_load_4d(st + mt * g.a_tile, &xmap, full + s, chunk * g.KC, tx[mt] + dx, ty[mt] + dy, tn[mt]);
-      tma_load_3d(st + kTcMTiles * g.a_tile, &wmap, full + s, chunk * g.KC, tap, 0);
-      issued = kb + 1;
-    }
-  } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer
-    const uint32_t idesc = idesc_bf16(128, g.nc);
-    const uint32_t sb = smem_u32(smem);
-    const uint32_t sbo = 16u * (uint32_t)g.KC;  // 8 rows of KC bf16
-    int kb = 0;
-    for (; kb < kblocks; kb++) {
-      const int s = kb % g.stages;
-      const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
-      if (!mbar_wait(full + s, ph, abort, true, 2u)) break;
-      tc_fence_after();
-      const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + kTcMTiles * g.a_tile;
-      for (int mt = 0; mt < mt_n; mt++) {
-        for (int j = 0; j < g.KC / 16; j++) {
-          const uint64_t ad = smem_desc_sw(a0 + mt * g.a_tile + 32 * j, sbo, g.swz);
-          const uint64_t bd = smem_desc_sw(b0 + 32 * j, sbo, g.swz);
-          umma_bf16(tmem + mt * g.col_stride, ad, bd, idesc, (kb > 0 || j > 0) ? 1u : 0u);
+        for (int mt = 0; mt < kTcMTiles; mt++) {
+          const int t = tile0 + mt, q = t % tiles_per_img;
+          tn[mt] = t / tiles_per_img;
+          ty[mt] = (q / (g.W / g.TW)) * g.R;
+          tx[mt] = (q % (g.W / g.TW)) * g.TW;
         }
+        const uint32_t bytes = (uint32_t)mt_n * g.a_tile + g.b_bytes;
+        bool ok = true;
+        for (int kb = 0; kb < kblocks; kb++, kbg++) {
+          const int s = kbg % g.stages;
+          const uint32_t ph = (uint32_t)(kbg / g.stages) & 1u;
+          if (!mbar_wait(empty + s, ph ^ 1u, abort, true, 1u)) {
+            ok = false;
+            break;
+          }
+          const int tap = kb / g.chunks, chunk = kb % g.chunks;
+          const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+          unsigned char* st = smem + s * g.stage_bytes;
+          mbar_expect_tx(full + s, bytes);
+          for (int mt = 0; mt < mt_n; mt++)
+            tma_load_4d(st + mt * g.a_tile, &xmap, full + s, chunk * g.KC, tx[mt] + dx, ty[mt] + dy, tn[mt]);
+          tma_load_3d(st + kTcMTiles * g.a_tile, &wmap, full + s, chunk * g.KC, tap, 0);
+          issued = kbg + 1;
+        }
+        if (!ok) break;
       }
-      umma_commit(empty + s);  // the stage is free once these MMAs have read it
     }
-    *consumed = kb;
-    umma_commit(accum);  // every MMA issued, done or not, before the accumulators are read
-  }
-
-  // ---- epilogue: all four warps, warp w reads TMEM lanes 32w..32w+31
-  __syncwarp();
-  const bool have = mbar_wait(accum, 0u, abort, false, 3u);
-  tc_fence_after();
-  // warp-uniform: the TMEM loads below are .sync.aligned
-  if (__all_sync(0xffffffffu, have && *abort == 0)) {
-    for (int mt = 0; mt < mt_n; mt++) {
-      // TMEM lane l of the tile is image pixel (ty + l / TW, tx + l % TW)
-      const int t = tile0 + mt, tiles_per_img = (g.H * g.W) >> 7;
-      const int q = t % tiles_per_img, l = warp * 32 + lane;
-      const long pix = ((long)(t / tiles_per_img) * g.H + (q / (g.W / g.TW)) * g.R + l / g.TW) * g.W +
-                       (q % (g.W / g.TW)) * g.TW + l % g.TW;
-      for (int j = 0; j < g.nc / 16; j++) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + mt * g.col_stride + 16 * j, v);
-        if (bias) {
-#pragma unroll
-          for (int i = 0; i < 16; i++) v[i] += bias[16 * j + i];
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      const uint32_t idesc = idesc_bf16(128, g.nc);
+      const uint32_t sb = smem_u32(smem);
+      const uint32_t sbo = 16u * (uint32_t)g.KC;  // 8 rows of KC bf16
+      int kbg = 0, it = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < g.pairs && ok; u += gridDim.x, it++) {
+        const int mt_n = min(kTcMTiles, g.tiles - u * kTcMTiles);
+        const int b = it % g.nbuf, use = it / g.nbuf;
+        if (!mbar_wait(tempty + b, (uint32_t)(use & 1) ^ 1u, abort, true, 5u)) break;
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * kTcMTiles * g.col_stride);
+        for (int kb = 0; kb < kblocks; kb++, kbg++) {
+          const int s = kbg % g.stages;
+          const uint32_t ph = (uint32_t)(kbg / g.stages) & 1u;
+          if (!mbar_wait(full + s, ph, abort, true, 2u)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + kTcMTiles * g.a_tile;
+          for (int mt = 0; mt < mt_n; mt++) {
+            for (int j = 0; j < g.KC / 16; j++) {
+              const uint64_t ad = smem_desc_sw(a0 + mt * g.a_tile + 32 * j, sbo, g.swz);
+              const uint64_t bd = smem_desc_sw(b0 + 32 * j, sbo, g.swz);
+              umma_bf16(acc + mt * g.col_stride, ad, bd, idesc, (kb > 0 || j > 0) ? 1u : 0u);
+            }
+          }
+          umma_commit(empty + s);  // the stage is free once these MMAs have read it
         }
-        uint4 o0, o1;
-        o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
-        o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
-        o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
-        o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
-        uint4* dst = reinterpret_cast<uint4*>(y + pix * g.nc + 16 * j);
-        dst[0] = o0;
-        dst[1] = o1;
-        if (act) {
-          // GELU of the bf16-rounded pre-activation, as the separate GELU pass computes it
+        umma_commit(tfull + b);  // the unit's accumulators are complete (or the unit was cut short)
+      }
+      *consumed = kbg;
+      umma_commit(drain);
+      mbar_wait(drain, 0u, abort, false, 6u);
+    }
+  } else {
+    // ---- epilogue: warps 2-5; warp w reads TMEM lanes 32 (w % 4) .. + 31
+    const int q4 = warp & 3, l = q4 * 32 + lane;
+    int it = 0;
+    for (int u = blockIdx.x; u < g.pairs; u += gridDim.x, it++) {
+      const int tile0 = u * kTcMTiles, mt_n = min(kTcMTiles, g.tiles - tile0);
+      const int b = it % g.nbuf, use = it / g.nbuf;
+      const bool have = mbar_wait(tfull + b, (uint32_t)(use & 1), abort, true, 3u);
+      tc_fence_after();
+      if (!__all_sync(0xffffffffu, have && *abort == 0)) break;
+      const uint32_t acc = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kTcMTiles * g.col_stride);
+      for (int mt = 0; mt < mt_n; mt++) {
+        // TMEM lane l of the tile is image pixel (ty + l / TW, tx + l % TW)
+        const int t = tile0 + mt, qq = t % tiles_per_img;
+        const long pix = ((long)(t / tiles_per_img) * g.H + (qq / (g.W / g.TW)) * g.R + l / g.TW) * g.W +
+                         (qq % (g.W / g.TW)) * g.TW + l % g.TW;
+        for (int j = 0; j < g.nc / 16; j++) {
+          float v[16];
+          tmem_ld16(acc + mt * g.col_stride + 16 * j, v);
+          if (bias) {
 #pragma unroll
-          for (int i = 0; i < 16; i++) v[i] = gelu_erf(__bfloat162float(__float2bfloat16_rn(v[i])));
+            for (int i = 0; i < 16; i++) v[i] += bias[16 * j + i];
+          }
+          uint4 o0, o1;
           o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
           o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
           o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
           o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
-          uint4* da = reinterpret_cast<uint4*>(act + pix * g.nc + 16 * j);
-          da[0] = o0;
-          da[1] = o1;
+          uint4* dst = reinterpret_cast<uint4*>(y + pix * g.nc + 16 * j);
+          dst[0] = o0;
+          dst[1] = o1;
+          if (act) {
+            // GELU of the bf16-rounded pre-activation, as the separate GELU pass computes it
+#pragma unroll
+            for (int i = 0; i < 16; i++) v[i] = gelu_erf(__bfloat162float(__float2bfloat16_rn(v[i])));
+            o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
+            o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
+            o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
+            o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
+            uint4* da = reinterpret_cast<uint4*>(act + pix * g.nc + 16 * j);
+            da[0] = o0;
+            da[1] = o1;
+          }
         }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty + b);  // this warp's quarter of set b is free
     }
   }
 
@@ -347,7 +394,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 struct TcWgradGeom {
   int H, W, cin, cout;
   int TW, R;          // a pixel tile: R image rows x TW pixels = 128 pixels
-  int cw, cr;         // a 16-pixel chunk of the tile: cr rows x cw pixels
   int MA, MB;         // channels per swizzled row of dy (A) and of x (B): 64, 32 or 16
   uint32_t swzA, swzB;
   int tiles;          // 128-pixel tiles in the batch
@@ -364,10 +410,11 @@ struct TcWgradGeom {
 // as a GEMM per tap with M = output channels (padded to 128; the rows past
 // cout are never stored), N = input channels, K = pixels, split over CTAs by
 // pixel tiles and over blockIdx.y by rows of taps. Both operands are
-// MN-major (channels contiguous) in the canonical swizzled layout: for each
-// 16-pixel K step, a TMA box of MA (or MB) channels x 16 pixels is 16 rows of
-// MA*2 bytes (8-row atoms SBO = 16*MA bytes apart along K), the next MA
-// channels one box further on (LBO = 32*MA bytes along M or N). Per k-block
+// MN-major (channels contiguous) in the canonical swizzled layout: a TMA box
+// of MA (or MB) channels x the tile's 128 pixels is 128 rows of MA*2 bytes
+// along K (8-row atoms SBO = 16*MA bytes apart; a 16-pixel K step is two of
+// them), the next MA channels one box further on (LBO = 256*MA bytes along M
+// or N). Per k-block
 // (one 128-pixel tile, one tap) the TMA brings the dy tile and the
 // tap-shifted x tile (zeros past the map edge). The partial sums leave TMEM
 // through fp32 atomics into dw.
@@ -425,15 +472,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const int dy = tap / 3 - 1, dx = tap % 3 - 1;
       unsigned char* st = smem + s * g.stage_bytes;
       mbar_expect_tx(full + s, bytes);
-      for (int k16 = 0; k16 < 8; k16++) {
-        // tile pixels 16 k16 .. 16 k16 + 15: cr rows of cw pixels
-        const int cx = tx + (16 * k16) % g.TW, cy = ty + (16 * k16) / g.TW;
-        unsigned char* a = st + k16 * 32 * g.cout;
-        unsigned char* b = st + g.a_bytes + k16 * 32 * g.cin;
-        for (int m = 0; m < g.cout / g.MA; m++) tma_load_4d(a + m * 32 * g.MA, &dymap, full + s, m * g.MA, cx, cy, tn);
-        for (int m = 0; m < g.cin / g.MB; m++)
-          tma_load_4d(b + m * 32 * g.MB, &xmap, full + s, m * g.MB, cx + dx, cy + dy, tn);
-      }
+      // one box per MA (MB) channels: the tile's 128 pixels as 128 rows
+      for (int m = 0; m < g.cout / g.MA; m++)
+        tma_load_4d(st + m * 256 * g.MA, &dymap, full + s, m * g.MA, tx, ty, tn);
+      for (int m = 0; m < g.cin / g.MB; m++)
+        tma_load_4d(st + g.a_bytes + m * 256 * g.MB, &xmap, full + s, m * g.MB, tx + dx, ty + dy, tn);
       issued = kb + 1;
     }
   } else if (warp == 1 && lane == 0) {
@@ -449,8 +492,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + g.a_bytes;
 #pragma unroll
       for (int k16 = 0; k16 < 8; k16++) {
-        const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.cout, 32 * g.MA, 16 * g.MA, g.swzA);
-        const uint64_t bd = smem_desc_full(b0 + k16 * 32 * g.cin, 32 * g.MB, 16 * g.MB, g.swzB);
+        const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.MA, 256 * g.MA, 16 * g.MA, g.swzA);
+        const uint64_t bd = smem_desc_full(b0 + k16 * 32 * g.MB, 256 * g.MB, 16 * g.MB, g.swzB);
         umma_bf16(tmem + j * g.col_stride, ad, bd, idesc, (i > 0 || k16 > 0) ? 1u : 0u);
       }
       umma_commit(empty + s);
@@ -563,17 +606,21 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   g.chunks = kc / g.KC;
   const long pixels = (long)N * H * W;
   g.tiles = (int)(pixels / 128);
+  g.pairs = (g.tiles + kTcMTiles - 1) / kTcMTiles;
   g.col_stride = (nc + 31) / 32 * 32;
+  g.nbuf = 2 * kTcMTiles * g.col_stride <= 512 ? 2 : 1;
   int cols = 32;
-  while (cols < kTcMTiles * g.col_stride) cols <<= 1;
+  while (cols < g.nbuf * kTcMTiles * g.col_stride) cols <<= 1;
   g.ncols = cols;
   g.a_tile = 128 * g.KC * 2;
   g.b_bytes = nc * g.KC * 2;
   g.stage_bytes = (kTcMTiles * g.a_tile + g.b_bytes + 1023) / 1024 * 1024;
   g.swz = g.KC == 64 ? 2u : (g.KC == 32 ? 4u : 6u);
-  g.stages = 4;
-  while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + 128 > 220 * 1024) g.stages--;
-  const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + 128;
+  g.stages = 6;
+  while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + 256 > 200 * 1024) g.stages--;
+  // At least 120 KiB, so that one CTA holds an SM (its TMEM allocation may be all 512 columns).
+  size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + 256;
+  if (smem < 120 * 1024) smem = 120 * 1024;
   if (smem > 227 * 1024) return cudaErrorNotSupported;
 
   CUtensorMap xm, wm;
@@ -588,8 +635,11 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int grid = (g.tiles + kTcMTiles - 1) / kTcMTiles;
-  k_conv_tc<<<grid, kTcThreads, smem, s>>>(xm, wm, bias, static_cast<bf16*>(y), static_cast<bf16*>(act), g);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = g.pairs < sms ? g.pairs : (sms > 0 ? sms : 1);
+  k_conv_tc<<<grid, kConvWarps * 32, smem, s>>>(xm, wm, bias, static_cast<bf16*>(y), static_cast<bf16*>(act), g);
   return cudaGetLastError();
 }
 
@@ -608,8 +658,6 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   g.cout = cout;
   g.TW = tile_width(W);
   g.R = 128 / g.TW;
-  g.cw = g.TW < 16 ? g.TW : 16;
-  g.cr = 16 / g.cw;
   g.MA = cout % 64 == 0 ? 64 : (cout % 32 == 0 ? 32 : 16);
   g.MB = cin % 64 == 0 ? 64 : (cin % 32 == 0 ? 32 : 16);
   g.swzA = g.MA == 64 ? 2u : (g.MA == 32 ? 4u : 6u);
@@ -622,8 +670,9 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   g.ncols = cols;
   g.a_bytes = 256 * cout;  // 8 K steps x 16 pixels x cout x 2 bytes
   g.stage_bytes = g.a_bytes + 256 * cin;
-  // the MMA reads 128 rows of A from the last K step: up to 4 KiB past its start
-  g.tail = 4096;
+  // the MMA reads 128 rows of A (128 / MA blocks of 256 MA bytes = 32 KiB from
+  // the stage's start): keep the last stage's reads inside the allocation
+  g.tail = g.stage_bytes < 32768 ? 32768 - g.stage_bytes : 0;
   g.stages = 4;
   while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128 > 200 * 1024) g.stages--;
   const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;
@@ -637,10 +686,10 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   CUtensorMap xm, dm;
   const cuuint64_t xd[4] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
   const cuuint64_t xs[3] = {(cuuint64_t)cin * 2, (cuuint64_t)W * cin * 2, (cuuint64_t)H * W * cin * 2};
-  const cuuint32_t xb[4] = {(cuuint32_t)g.MB, (cuuint32_t)g.cw, (cuuint32_t)g.cr, 1};
+  const cuuint32_t xb[4] = {(cuuint32_t)g.MB, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
   const cuuint64_t dd[4] = {(cuuint64_t)cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
   const cuuint64_t ds[3] = {(cuuint64_t)cout * 2, (cuuint64_t)W * cout * 2, (cuuint64_t)H * W * cout * 2};
-  const cuuint32_t db[4] = {(cuuint32_t)g.MA, (cuuint32_t)g.cw, (cuuint32_t)g.cr, 1};
+  const cuuint32_t db[4] = {(cuuint32_t)g.MA, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
   cudaError_t e = make_map(&xm, x, 4, xd, xs, xb, g.MB * 2);
   if (e == cudaSuccess) e = make_map(&dm, dy, 4, dd, ds, db, g.MA * 2);
   if (e != cudaSuccess) return e;
