@@ -89,10 +89,6 @@ __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
   return old;
 }
 
-__device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // Grid-wide barrier of a cooperative launch (all blocks co-resident), one
 // arrival atomic per block: every block adds 1 to the flip counter but block
 // 0, which adds 2^31 - (blocks - 1), so the counter's top bit flips exactly
@@ -130,16 +126,35 @@ __device__ bool grid_sync(GridBarrier* gb, unsigned int* status, unsigned long l
   return s_ok != 0;
 }
 
-// A grid barrier of one atomic per block whose arrivals also add up one
-// count per block. Block 0 adds 2^31 - (blocks - 1) to the flip counter and
-// every other block 1, so the counter's top bit flips exactly when the last
-// block arrives and each block waits for the flip relative to the value its
-// own arrival returned: no generation word to read first or to publish last.
-// The counts go to sums[phase] (phase = step mod 3): *below gets the sum over
-// the blocks whose counts landed before this one's (an arrival order standing
-// in for a block order), *total the sum over all blocks, read after the flip.
-// Block 0 clears sums[phase + 1 mod 3] before it arrives: that counter's last
-// total was read two barriers ago, and its next counts come after this one.
+// A grid barrier of one 64-bit atomic per block whose arrivals also add up
+// one count per block. The word sums[phase] (phase = step mod 3, one 128-byte
+// line each) holds the arrivals in its high half and the counts in its low
+// half; a block adds 2^32 + its count and waits until the high half shows
+// every block. *below gets the counts of the blocks whose arrivals landed
+// before this one's (an arrival order standing in for a block order),
+// *total the sum over all blocks, from the same word. Block 0 clears the
+// word of phase + 1 mod 3 before it arrives: that word's last total was read
+// two barriers ago, and its next arrivals come after this barrier. The poll
+// reads the abort flag (relaxed) ahead of the word (acquire), so that the two
+// loads overlap; the last block to arrive reads neither.
+__device__ __forceinline__ unsigned long long atom_add_acq_rel64(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned ld_relaxed32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned long long limit, unsigned phase,
                               unsigned mine, unsigned* below, unsigned* total) {
   __shared__ int s_ok;
@@ -147,27 +162,37 @@ __device__ bool grid_sync_sum(GridBarrier* gb, unsigned int* status, unsigned lo
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    unsigned* sum = &gb->sums[32 * phase];
-    if (blockIdx.x == 0) st_relaxed(&gb->sums[32 * (phase == 2 ? 0 : phase + 1)], 0u);
-    const unsigned b = atomicAdd(sum, mine);
-    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
-    const unsigned old = atom_add_acq_rel(&gb->flip, add);
-    const unsigned long long t0 = global_ns();
-    while (((ld_acquire(&gb->flip) ^ old) & 0x80000000u) == 0) {
-      if (ld_acquire(&gb->abort)) {
+    unsigned long long* word = reinterpret_cast<unsigned long long*>(&gb->sums[32 * phase]);
+    if (blockIdx.x == 0) {
+      unsigned long long* next = reinterpret_cast<unsigned long long*>(&gb->sums[32 * (phase == 2 ? 0 : phase + 1)]);
+      asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(next), "l"(0ull) : "memory");
+    }
+    const unsigned long long add = (1ull << 32) | mine;
+    const unsigned long long old = atom_add_acq_rel64(word, add);
+    const unsigned long long all = (unsigned long long)gridDim.x << 32;
+    unsigned long long v = old + add;
+    unsigned long long t0 = 0;
+    for (unsigned i = 0; (v & 0xFFFFFFFF00000000ull) != all; i++) {
+      const unsigned ab = ld_relaxed32(&gb->abort);
+      v = ld_acquire64(word);
+      if (ab) {
         ok = 0;
         break;
       }
-      if (global_ns() - t0 > limit) {
-        atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
-        atomicExch(&gb->abort, 1u);
-        ok = 0;
-        break;
+      if ((i & 15u) == 15u) {
+        const unsigned long long now = global_ns();
+        if (t0 == 0) {
+          t0 = now;
+        } else if (now - t0 > limit) {
+          atomicOr(status, 0x8u);  // SWE_STATUS_TIMEOUT
+          atomicExch(&gb->abort, 1u);
+          ok = 0;
+          break;
+        }
       }
     }
-    if (ld_acquire(&gb->abort)) ok = 0;
-    s_below = b;
-    s_total = ld_acquire(sum);
+    s_below = (unsigned)old;
+    s_total = (unsigned)v;
     s_ok = ok;
   }
   __syncthreads();
@@ -1034,7 +1059,9 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   __shared__ int s_free[2];            // free lanes of this CTA by step parity, read by the other CTAs
   __shared__ int s_all[kClusterCtas];  // every CTA's free lanes, this step (clusters of up to 16 CTAs)
   __shared__ int s_warp[32];
-  __shared__ unsigned long long s_time[3];  // fly, cascades, last mark (CTA 0's thread 0)
+  // CTA 0's thread 0: flights + barrier, absorbs + cascades, last mark, tag
+  // waits of the flights, barrier, refill + absorbs
+  __shared__ unsigned long long s_time[6];
   const int T = blockDim.x;
   const int cap = slots * T;
   // Particle fields (id, age, sed_q, px, py, pz, vx, vy, vz) of lane slot j.
@@ -1044,6 +1071,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   int* s_vis = dyn + 10 * cap;       // per lane slot: cascades the owned cell owes
   int* s_ox = dyn + 11 * cap;        // per lane slot: the owned cell's x
   int32_t* N = dyn + 12 * cap + 9 * threadIdx.x;  // this thread's 3x3 neighbourhood
+  // per lane slot and step parity: the cell the slot marked visited (-1: none)
+  int* s_mark = dyn + 12 * cap + 9 * T;
   // Per cell colour (x%3, z%3): the cells of the 5x5 block around (bit
   // (du+2)*5 + dw+2) whose colour is lower.
   __shared__ unsigned s_lower[9];
@@ -1082,9 +1111,15 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
 
   const bool timer = r == 0 && t == 0;
   if (timer) {
-    s_time[0] = 0;
-    s_time[1] = 0;
+    for (int k = 0; k < 6; k++) s_time[k] = 0;
     s_time[2] = global_ns();
+  }
+#pragma unroll
+  for (int s = 0; s < kClusterMaxSlots; s++) {
+    if (s < slots) {
+      s_mark[2 * (s * T + t)] = -1;
+      s_mark[2 * (s * T + t) + 1] = -1;
+    }
   }
 
   unsigned ph = 0;  // barriers passed
@@ -1175,12 +1210,21 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
     const unsigned tbase = 16u * (step + 1);  // tag base of this step
     // visited bitmaps by step mod 3: this step's, the previous step's, and
     // the one two steps back, cleared now (its last readers were the
-    // previous step's flights; its next writers fly after this step's barrier)
+    // previous step's flights; its next writers fly after this step's
+    // barrier): every lane slot clears the word of the cell it marked then,
+    // so every set bit is cleared, word by word
     uint32_t* vb = B.vbits[rot];
     const uint32_t* vb_prev = B.vbits[rot == 0 ? 2 : rot - 1];
     {
       uint32_t* vb_clear = B.vbits[rot == 2 ? 0 : rot + 1];
-      for (long i = (long)r * T + t; i < B.vbits_words; i += (long)nb * T) vb_clear[i] = 0;
+#pragma unroll
+      for (int s = 0; s < kClusterMaxSlots; s++) {
+        if (s < slots) {
+          const int m = s_mark[2 * (s * T + t) + (step & 1u)];
+          if (m >= 0) vb_clear[((long)m + 64) >> 5] = 0u;
+          s_mark[2 * (s * T + t) + (step & 1u)] = -1;
+        }
+      }
     }
     int32_t* visits = odd ? B.visits2 : B.visits;
     int32_t* dq = odd ? B.dq2 : B.dq;
@@ -1268,6 +1312,12 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
         if (!__any_sync(0xffffffffu, ready != need)) break;
         __nanosleep(64);
       }
+      if (timer) {
+        const unsigned long long now = global_ns();
+        s_time[0] += now - s_time[2];
+        s_time[3] += now - s_time[2];
+        s_time[2] = now;
+      }
       if ((live >> s) & 1u) {
         if (ci >= 0 && !gave_up)
           ci = fly_from(c, B, dq, ci, ix, iz, hv[0], hv[1], hv[2], hv[3], hv[4], c_lo, c_hi, A.seed_lo, A.seed_hi,
@@ -1281,6 +1331,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           atomicAdd(visits + ci, 1);
           atomicMin(owner + ci, lane_id0 + j);
           mark_visited(vb, ci);
+          s_mark[2 * j + (step & 1u)] = (int)ci;
           s_own[j] = (int)ci;
           s_ox[j] = ix;
           flew |= 1u << s;
@@ -1296,6 +1347,11 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
 
     // The step's one barrier: every exchange and visit of the step is in,
     // and the free lanes are counted on the way.
+    if (timer) {
+      const unsigned long long now = global_ns();
+      s_time[0] += now - s_time[2];
+      s_time[2] = now;
+    }
     const unsigned freem = lanes_mask & ~live;
     int btotal = 0;
     const int pre = block_scan(__popc(freem), &btotal);
@@ -1322,6 +1378,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
     if (timer) {
       const unsigned long long now = global_ns();
       s_time[0] += now - s_time[2];
+      s_time[4] += now - s_time[2];
       s_time[2] = now;
     }
     const int survivors = L - total_free;
@@ -1358,6 +1415,12 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
           st_relaxed64(HW + ci, make_word(wrap_add(word_height(w), d), tbase + 1));
         }
       }
+    }
+    if (timer) {
+      const unsigned long long now = global_ns();
+      s_time[1] += now - s_time[2];
+      s_time[5] += now - s_time[2];
+      s_time[2] = now;
     }
     // Cascades of the owned cells. Each lane takes its cells in colour order
     // (lowest first) and cascades one as soon as the tags of its 3x3 words
@@ -1541,6 +1604,9 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
     cnt->cascade_ns += s_time[1];
     cnt->phase_ns[1] += s_time[0];
     cnt->phase_ns[3] += s_time[1];
+    cnt->phase_ns[0] += s_time[3];
+    cnt->phase_ns[2] += s_time[4];
+    cnt->phase_ns[4] += s_time[5];
   }
 }
 
@@ -1668,9 +1734,10 @@ bool lanes_shape(int lanes, int ctas, int max_threads, int* threads, int* slots)
   return true;
 }
 
-// particle state (9 words) and owned cell, owed cascades and the cell's x
-// (3 words) per lane slot, and a 3x3 neighbourhood per thread
-size_t lanes_smem(int threads, int slots) { return sizeof(int32_t) * (size_t)threads * (12 * slots + 9); }
+// particle state (9 words), owned cell, owed cascades, the cell's x and the
+// cells marked visited in the last two steps (5 words) per lane slot, and a
+// 3x3 neighbourhood per thread
+size_t lanes_smem(int threads, int slots) { return sizeof(int32_t) * (size_t)threads * (14 * slots + 9); }
 
 cudaError_t launch_cluster(const CycleArgs& A, int threads, int slots, cudaStream_t s, bool* launched) {
   *launched = false;
