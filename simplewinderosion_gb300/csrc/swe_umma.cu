@@ -201,7 +201,12 @@ struct TcConvGeom {
   uint32_t swz;    // descriptor layout code of the swizzle
 };
 
-constexpr int kConvWarps = 6;  // warp 0 copies, warp 1 issues the MMAs, warps 2-5 run the epilogue
+// warp 0 copies, warp 1 issues the MMAs, warps 2-9 run the epilogue: two
+// warps per TMEM lane quarter (warp w may read lanes 32 (w % 4) .. + 31),
+// each taking every other 16-column chunk, so that every SM sub-partition
+// issues the epilogue's conversions from two warps
+constexpr int kConvWarps = 10;
+constexpr int kConvEpilogueWarps = kConvWarps - 2;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(tfull + b, 1);
-      mbar_init(tempty + b, 4);
+      mbar_init(tempty + b, kConvEpilogueWarps);
     }
     mbar_init(drain, 1);
     *abort = 0;
@@ -330,8 +335,9 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
       mbar_wait(drain, 0u, abort, false, 6u);
     }
   } else {
-    // ---- epilogue: warps 2-5; warp w reads TMEM lanes 32 (w % 4) .. + 31
-    const int q4 = warp & 3, l = q4 * 32 + lane;
+    // ---- epilogue: warps 2-9; warp w reads TMEM lanes 32 (w % 4) .. + 31,
+    // chunks j = (w - 2) / 4, + 2, ...
+    const int q4 = warp & 3, l = q4 * 32 + lane, half = (warp - 2) >> 2;
     int it = 0;
     for (int u = blockIdx.x; u < g.pairs; u += gridDim.x, it++) {
       const int tile0 = u * kTcMTiles, mt_n = min(kTcMTiles, g.tiles - tile0);
@@ -345,7 +351,7 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
         const int t = tile0 + mt, qq = t % tiles_per_img;
         const long pix = ((long)(t / tiles_per_img) * g.H + (qq / (g.W / g.TW)) * g.R + l / g.TW) * g.W +
                          (qq % (g.W / g.TW)) * g.TW + l % g.TW;
-        for (int j = 0; j < g.nc / 16; j++) {
+        for (int j = half; j < g.nc / 16; j += 2) {
           float v[16];
           tmem_ld16(acc + mt * g.col_stride + 16 * j, v);
           if (bias) {
@@ -376,7 +382,7 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(tempty + b);  // this warp's quarter of set b is free
+      if (lane == 0) mbar_arrive(tempty + b);  // this warp is done with set b
     }
   }
 
@@ -399,6 +405,7 @@ struct TcWgradGeom {
   int tiles;          // 128-pixel tiles in the batch
   int tiles_per_cta;  // the CTA's share of the pixel sum (split K)
   int taps;           // taps per CTA (9, or 3: one row of taps per blockIdx.y)
+  int kt;             // taps per k-block: one dy tile serves kt tap-shifted x tiles (kt divides taps)
   int col_stride;     // TMEM columns per tap
   int ncols;
   int stages;
@@ -414,10 +421,9 @@ struct TcWgradGeom {
 // of MA (or MB) channels x the tile's 128 pixels is 128 rows of MA*2 bytes
 // along K (8-row atoms SBO = 16*MA bytes apart; a 16-pixel K step is two of
 // them), the next MA channels one box further on (LBO = 256*MA bytes along M
-// or N). Per k-block
-// (one 128-pixel tile, one tap) the TMA brings the dy tile and the
-// tap-shifted x tile (zeros past the map edge). The partial sums leave TMEM
-// through fp32 atomics into dw.
+// or N). Per k-block (one 128-pixel tile, kt taps) the TMA brings the dy
+// tile once and the kt tap-shifted x tiles (zeros past the map edge). The
+// partial sums leave TMEM through fp32 atomics into dw.
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap,
                float* __restrict__ dw, const TcWgradGeom g) {
@@ -435,7 +441,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int t0 = blockIdx.x * g.tiles_per_cta;
   const int nt = max(0, min(g.tiles_per_cta, g.tiles - t0));
   const int tap0 = blockIdx.y * g.taps;
-  const int kblocks = nt * g.taps;
+  const int gk = g.taps / g.kt;  // k-blocks per tile
+  const int kblocks = nt * gk;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < g.stages; s++) {
@@ -461,22 +468,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   int issued = 0;
   if (warp == 0 && lane == 0) {
     const int tiles_per_img = (g.H * g.W) >> 7;
-    const uint32_t bytes = 256u * (uint32_t)(g.cout + g.cin);  // 8 K steps x 16 pixels x channels x 2 bytes
+    // 8 K steps x 16 pixels x channels x 2 bytes: the dy tile and kt x tiles
+    const uint32_t bytes = 256u * (uint32_t)(g.cout + g.kt * g.cin);
     for (int kb = 0; kb < kblocks; kb++) {
       const int s = kb % g.stages;
       const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
       if (!mbar_wait(empty + s, ph ^ 1u, abort, true, 11u)) break;
-      const int t = t0 + kb / g.taps, tap = tap0 + kb % g.taps;
+      const int t = t0 + kb / gk, tapk = tap0 + (kb % gk) * g.kt;
       const int q = t % tiles_per_img, tn = t / tiles_per_img;
       const int ty = (q / (g.W / g.TW)) * g.R, tx = (q % (g.W / g.TW)) * g.TW;
-      const int dy = tap / 3 - 1, dx = tap % 3 - 1;
       unsigned char* st = smem + s * g.stage_bytes;
       mbar_expect_tx(full + s, bytes);
       // one box per MA (MB) channels: the tile's 128 pixels as 128 rows
       for (int m = 0; m < g.cout / g.MA; m++)
         tma_load_4d(st + m * 256 * g.MA, &dymap, full + s, m * g.MA, tx, ty, tn);
-      for (int m = 0; m < g.cin / g.MB; m++)
-        tma_load_4d(st + g.a_bytes + m * 256 * g.MB, &xmap, full + s, m * g.MB, tx + dx, ty + dy, tn);
+      for (int k = 0; k < g.kt; k++) {
+        const int dy = (tapk + k) / 3 - 1, dx = (tapk + k) % 3 - 1;
+        unsigned char* xs = st + g.a_bytes + k * 256 * g.cin;
+        for (int m = 0; m < g.cin / g.MB; m++)
+          tma_load_4d(xs + m * 256 * g.MB, &xmap, full + s, m * g.MB, tx + dx, ty + dy, tn);
+      }
       issued = kb + 1;
     }
   } else if (warp == 1 && lane == 0) {
@@ -488,13 +499,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint32_t ph = (uint32_t)(kb / g.stages) & 1u;
       if (!mbar_wait(full + s, ph, abort, true, 12u)) break;
       tc_fence_after();
-      const int i = kb / g.taps, j = kb % g.taps;
-      const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + g.a_bytes;
+      const int i = kb / gk, j0 = (kb % gk) * g.kt;
+      const uint32_t a0 = sb + s * g.stage_bytes;
+      for (int k = 0; k < g.kt; k++) {
+        const uint32_t b0 = a0 + g.a_bytes + k * 256 * g.cin;
 #pragma unroll
-      for (int k16 = 0; k16 < 8; k16++) {
-        const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.MA, 256 * g.MA, 16 * g.MA, g.swzA);
-        const uint64_t bd = smem_desc_full(b0 + k16 * 32 * g.MB, 256 * g.MB, 16 * g.MB, g.swzB);
-        umma_bf16(tmem + j * g.col_stride, ad, bd, idesc, (i > 0 || k16 > 0) ? 1u : 0u);
+        for (int k16 = 0; k16 < 8; k16++) {
+          const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.MA, 256 * g.MA, 16 * g.MA, g.swzA);
+          const uint64_t bd = smem_desc_full(b0 + k16 * 32 * g.MB, 256 * g.MB, 16 * g.MB, g.swzB);
+          umma_bf16(tmem + (j0 + k) * g.col_stride, ad, bd, idesc, (i > 0 || k16 > 0) ? 1u : 0u);
+        }
       }
       umma_commit(empty + s);
     }
@@ -607,7 +621,8 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   const long pixels = (long)N * H * W;
   g.tiles = (int)(pixels / 128);
   g.pairs = (g.tiles + kTcMTiles - 1) / kTcMTiles;
-  g.col_stride = (nc + 31) / 32 * 32;
+  g.col_stride = 32;  // a power of two: every accumulator starts on a multiple of its width
+  while (g.col_stride < nc) g.col_stride <<= 1;
   g.nbuf = 2 * kTcMTiles * g.col_stride <= 512 ? 2 : 1;
   int cols = 32;
   while (cols < g.nbuf * kTcMTiles * g.col_stride) cols <<= 1;
@@ -669,10 +684,15 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   while (cols < g.taps * g.col_stride) cols <<= 1;
   g.ncols = cols;
   g.a_bytes = 256 * cout;  // 8 K steps x 16 pixels x cout x 2 bytes
-  g.stage_bytes = g.a_bytes + 256 * cin;
+  // the most taps per k-block (9, 3 or 1, dividing the CTA's taps) with which two stages fit
+  auto stage_of = [&](int kt) { return g.a_bytes + 256 * kt * cin; };
   // the MMA reads 128 rows of A (128 / MA blocks of 256 MA bytes = 32 KiB from
   // the stage's start): keep the last stage's reads inside the allocation
-  g.tail = g.stage_bytes < 32768 ? 32768 - g.stage_bytes : 0;
+  auto tail_of = [&](int kt) { return stage_of(kt) < 32768 ? 32768 - stage_of(kt) : 0; };
+  g.kt = g.taps;
+  while (g.kt > 1 && 1024 + 2 * (size_t)stage_of(g.kt) + tail_of(g.kt) + 128 > 200 * 1024) g.kt /= 3;
+  g.stage_bytes = stage_of(g.kt);
+  g.tail = tail_of(g.kt);
   g.stages = 4;
   while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128 > 200 * 1024) g.stages--;
   const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;

@@ -62,6 +62,25 @@ def test_tc_conv_forward_and_input_gradient(ops, shape):
     assert ops.status() == 0
 
 
+@pytest.mark.parametrize("shape", [
+    (8, 64, 256, 32, 96),   # 512 tile pairs: every CTA of the persistent grid takes 3-4, two accumulator sets
+    (5, 64, 256, 16, 256),  # 320 pairs with 256 output channels: one accumulator set, reused in turn
+])
+def test_tc_conv_persistent_many_units(ops, shape):
+    """More units (pairs of 128-pixel tiles) than SMs: each CTA runs the
+    stage ring through several units and reuses its TMEM accumulator sets."""
+    n, h, w, cin, cout = shape
+    rs = np.random.RandomState(cin + cout)
+    x = R.bf16(rs.standard_normal((n, h, w, cin)))
+    wt = R.bf16(rs.standard_normal((cout, 3, 3, cin)) * np.sqrt(2.0 / (9 * cin)))
+    b = rs.standard_normal(cout).astype(np.float32)
+    y, a = ops.conv_tc(dev(x), ops.pack_tc(dev(wt)), torch.from_numpy(b).cuda(), cout, act=True)
+    yh = host(y)
+    close(yh, R.conv3x3(x, wt, b))
+    close(host(a), R.gelu(yh))
+    assert ops.status() == 0
+
+
 def test_tc_conv_equals_warp_level_conv_closely(ops):
     """Same inputs through the tensor-core kernel and the warp-level mma.sync
     kernel: both accumulate bf16 products in fp32; outputs agree within one
