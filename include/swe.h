@@ -328,10 +328,12 @@ int swe_world_kernel_times(swe_world* w, double* fly_ms, double* cascade_ms);
 
 /* The same clock per phase of the parallel cycle kernels, ms summed over the
  * last swe_world_erode call, in the order: spawn, fly, (unused), colour 0..8,
- * ema (n <= 13 values written). The all-at-once kernel fills every slot; the
- * bounded-lanes kernel (the default) has no colour phases and reports its
- * flights and barrier under fly and its absorbs and cascades under colour 0
- * (its spawns, map sweeps and EMA are not timed). */
+ * ema (n <= 13 values written). The all-at-once kernel fills every slot. The
+ * bounded-lanes kernel (the default) has no colour phases; its slots hold:
+ * fly = flights, their tag waits and the step's barrier; colour 0 = refills,
+ * absorbs and cascades; and parts of those two: spawn = the flights' tag
+ * waits, (unused) = the barrier, colour 1 = refills and absorbs (its map
+ * sweeps and EMA are not timed). */
 int swe_world_phase_times(swe_world* w, double* ms, int n);
 
 /* Cascade work of the last parallel swe_world_erode call: World::cascade
@@ -439,6 +441,15 @@ int swe_nn_add(const void* a, const void* b, void* out, int64_t count, void* str
  * wind direction's x and z components (wind_xz: 2 floats per map), zeros.
  * height fp32 [n,h,w]. */
 int swe_nn_pack_input(const float* height, const float* wind_xz, void* x, int n, int h, int wd, void* stream);
+/* The same with every map's heights moved by a constant so that its mean is
+ * `ref`: channel 0 = ((height - mean) + (ref - 0.25)) * 4, mean = the map's
+ * mean height, also written to means (device, n floats). The erosion rules
+ * see heights only through differences (slopes, normals, the particle's
+ * height above the cell, cascades), so the change over a jump does not
+ * depend on such a constant; the network then sees every terrain at the
+ * height level it was trained on. */
+int swe_nn_pack_input_centered(const float* height, const float* wind_xz, float* means, void* x, int n, int h, int wd,
+                               float ref, void* stream);
 /* Squared error of channel 0 of pred (bf16 [pixels, c]) against target *
  * target_scale (target fp32 [pixels]): the sum of squares is ADDED to *loss
  * (device fp32) and dpred = 2 (pred - target target_scale) grad_scale on

@@ -79,10 +79,16 @@ def up2_bwd(dy):
     return dy.reshape(n, h // 2, 2, wd // 2, 2, c).sum(axis=(2, 4)).astype(np.float32)
 
 
-def pack_input(height, wind_xz):
+def pack_input(height, wind_xz, ref=None):
+    """swe_nn_pack_input; with ref, swe_nn_pack_input_centered (each map moved
+    so that its mean height is ref)."""
     n, h, wd = height.shape
     x = np.zeros((n, h, wd, 16), np.float32)
-    x[..., 0] = (height - np.float32(0.25)) * np.float32(4.0)
+    if ref is None:
+        x[..., 0] = (height - np.float32(0.25)) * np.float32(4.0)
+    else:
+        m = height.reshape(n, -1).astype(np.float64).mean(axis=1).astype(np.float32)[:, None, None]
+        x[..., 0] = ((height - m) + (np.float32(ref) - np.float32(0.25))) * np.float32(4.0)
     x[..., 1] = wind_xz[:, 0, None, None]
     x[..., 2] = wind_xz[:, 1, None, None]
     return x

@@ -172,7 +172,10 @@ cudaError_t nn_gelu_bwd(const void* pre, const void* dact, void* dpre, long n, c
 cudaError_t nn_pool2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s);
 cudaError_t nn_up2(const void* x, void* y, int N, int H, int W, int C, bool backward, cudaStream_t s);
 cudaError_t nn_add(const void* a, const void* b, void* out, long n, cudaStream_t s);
-cudaError_t nn_pack_input(const float* h, const float* wind_xz, void* x, int N, int H, int W, cudaStream_t s);
+// means (device, N floats) or nullptr: each map's mean, written first, and
+// the heights moved so that the mean is ref
+cudaError_t nn_pack_input(const float* h, const float* wind_xz, void* x, int N, int H, int W, cudaStream_t s,
+                          float* means, float ref);
 cudaError_t nn_mse(const void* pred, const float* target, float tscale, void* dpred, float* loss, long M, int C,
                    float gscale, cudaStream_t s);
 cudaError_t nn_channel0(const void* pred, float* out, long M, int C, float oscale, cudaStream_t s);

@@ -426,13 +426,15 @@ __global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf
 
 // Network input, 16 channels per pixel: (height - 0.25) * 4, the wind
 // direction's x and z components, zeros.
+// With means (per map, device), the heights are first moved so that each
+// map's mean is `ref`: ((h - mean) + (ref - 0.25)) * 4.
 __global__ void k_pack_input(const float* __restrict__ h, const float* __restrict__ wind_xz, bf16* __restrict__ x,
-                             int N, int H, int W) {
+                             int N, int H, int W, const float* __restrict__ means, float ref) {
   const long n = (long)N * H * W;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
     const long b = p / ((long)H * W);
     bf16* o = x + p * 16;
-    o[0] = __float2bfloat16_rn((h[p] - 0.25f) * 4.0f);
+    o[0] = __float2bfloat16_rn(means ? ((h[p] - means[b]) + (ref - 0.25f)) * 4.0f : (h[p] - 0.25f) * 4.0f);
     o[1] = __float2bfloat16_rn(wind_xz[2 * b]);
     o[2] = __float2bfloat16_rn(wind_xz[2 * b + 1]);
 #pragma unroll
@@ -590,8 +592,30 @@ cudaError_t nn_add(const void* a, const void* b, void* out, long n, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t nn_pack_input(const float* h, const float* wind_xz, void* x, int N, int H, int W, cudaStream_t s) {
-  k_pack_input<<<grid_for((long)N * H * W), 256, 0, s>>>(h, wind_xz, static_cast<bf16*>(x), N, H, W);
+// Mean of each of N maps of M floats, one CTA per map: per-thread float
+// partial sums in a fixed order, then a fixed-order block reduction in
+// double (the same result on every run).
+__global__ void __launch_bounds__(1024) k_map_mean(const float* __restrict__ h, long M, float* __restrict__ means) {
+  __shared__ double part[32];
+  const float* m = h + (long)blockIdx.x * M;
+  float acc = 0.0f;
+  for (long i = threadIdx.x; i < M; i += blockDim.x) acc += m[i];
+  double d = acc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+    means[blockIdx.x] = (float)(t / (double)M);
+  }
+}
+
+cudaError_t nn_pack_input(const float* h, const float* wind_xz, void* x, int N, int H, int W, cudaStream_t s,
+                          float* means, float ref) {
+  if (means) k_map_mean<<<N, 1024, 0, s>>>(h, (long)H * W, means);
+  k_pack_input<<<grid_for((long)N * H * W), 256, 0, s>>>(h, wind_xz, static_cast<bf16*>(x), N, H, W, means, ref);
   return cudaGetLastError();
 }
 
@@ -746,7 +770,14 @@ int swe_nn_add(const void* a, const void* b, void* out, int64_t count, void* str
 
 int swe_nn_pack_input(const float* height, const float* wind_xz, void* x, int n, int h, int wd, void* stream) {
   if (!height || !wind_xz || !x || n < 1 || h < 1 || wd < 1) return nn_fail(SWE_ERR_INVALID, "pack_input: bad arguments");
-  return nn_done(swe::nn_pack_input(height, wind_xz, x, n, h, wd, static_cast<cudaStream_t>(stream)));
+  return nn_done(swe::nn_pack_input(height, wind_xz, x, n, h, wd, static_cast<cudaStream_t>(stream), nullptr, 0.0f));
+}
+
+int swe_nn_pack_input_centered(const float* height, const float* wind_xz, float* means, void* x, int n, int h, int wd,
+                               float ref, void* stream) {
+  if (!height || !wind_xz || !means || !x || n < 1 || h < 1 || wd < 1 || !(ref == ref))
+    return nn_fail(SWE_ERR_INVALID, "pack_input_centered: bad arguments");
+  return nn_done(swe::nn_pack_input(height, wind_xz, x, n, h, wd, static_cast<cudaStream_t>(stream), means, ref));
 }
 
 int swe_nn_mse(const void* pred, const float* target, float target_scale, void* dpred, float* loss, int64_t pixels,

@@ -55,6 +55,7 @@ def _bind():
     L.swe_nn_up2.argtypes = [_P, _P, i32, i32, i32, i32, i32, _P]
     L.swe_nn_add.argtypes = [_P, _P, _P, i64, _P]
     L.swe_nn_pack_input.argtypes = [_P, _P, _P, i32, i32, i32, _P]
+    L.swe_nn_pack_input_centered.argtypes = [_P, _P, _P, _P, i32, i32, i32, f32, _P]
     L.swe_nn_mse.argtypes = [_P, _P, f32, _P, _P, i64, i32, f32, _P]
     L.swe_nn_channel0.argtypes = [_P, _P, i64, i32, f32, _P]
     L.swe_nn_adam.argtypes = [_P, _P, _P, _P, _P, i64, f32, f32, f32, f32, i32, _P]
@@ -177,24 +178,38 @@ class Ops:
         _check(lib.swe_nn_add(_p(a), _p(b), _p(y), a.numel(), self.s))
         return y
 
-    def pack(self, height, wind_xz):
+    def pack(self, height, wind_xz, ref=None):
+        """The network input; with `ref`, every map's heights are first moved
+        so that its mean is ref (swe_nn_pack_input_centered)."""
         n, h, wd = height.shape
         x = self.empty(n, h, wd, 16)
-        _check(lib.swe_nn_pack_input(_p(height), _p(wind_xz), _p(x), n, h, wd, self.s))
+        if ref is None:
+            _check(lib.swe_nn_pack_input(_p(height), _p(wind_xz), _p(x), n, h, wd, self.s))
+        else:
+            means = self.torch.empty(n, dtype=self.torch.float32, device=self.device)
+            _check(lib.swe_nn_pack_input_centered(_p(height), _p(wind_xz), _p(means), _p(x), n, h, wd, float(ref),
+                                                  self.s))
         return x
 
 
 class Surrogate:
     """The U-Net, its fp32 master weights, bf16 copies, gradients and Adam
-    moments. `scale`: the height change is predicted as change * scale."""
+    moments. `scale`: the height change is predicted as change * scale.
+    `height_ref`: every input map is moved by a constant so that its mean
+    height is height_ref (the erosion rules see only height differences, so
+    the change over a jump does not depend on that constant); training and
+    prediction both see terrains at that level."""
 
-    def __init__(self, device="cuda", seed=0, scale=100.0, use_tc=True):
+    HEIGHT_REF = 0.35  # about the mean height of the training terrains
+
+    def __init__(self, device="cuda", seed=0, scale=100.0, use_tc=True, height_ref=HEIGHT_REF):
         import torch
         self.torch = torch
         self.use_tc = use_tc  # tensor-core (tcgen05) convolutions where the shape allows
         self.device = torch.device(device)
         self.ops = Ops(torch, self.device)
         self.scale = float(scale)
+        self.height_ref = float(height_ref)
         rs = np.random.RandomState(seed)
         self.w, self.b, self.w16 = {}, {}, {}
         for name, cin, cout in LAYERS:
@@ -222,7 +237,7 @@ class Surrogate:
             _check(lib.swe_nn_to_bf16(_p(w), _p(self.w16[k]), w.numel(), self.ops.s))
 
     def state(self) -> dict:
-        out = {"scale": np.float32(self.scale)}
+        out = {"scale": np.float32(self.scale), "height_ref": np.float32(self.height_ref)}
         for k in self.w:
             out[f"w_{k}"] = self.w[k].cpu().numpy()
             out[f"b_{k}"] = self.b[k].cpu().numpy()
@@ -230,6 +245,8 @@ class Surrogate:
 
     def load(self, state: dict):
         self.scale = float(state["scale"])
+        if "height_ref" in state:
+            self.height_ref = float(state["height_ref"])
         for k in self.w:
             self.w[k].copy_(self.torch.from_numpy(np.asarray(state[f"w_{k}"], np.float32)))
             self.b[k].copy_(self.torch.from_numpy(np.asarray(state[f"b_{k}"], np.float32)))
@@ -337,7 +354,7 @@ class Surrogate:
         target_dh fp32 [n,h,w] (unscaled). Returns the mean squared error of
         the scaled prediction."""
         torch = self.torch
-        x = self.ops.pack(height, wind_xz)
+        x = self.ops.pack(height, wind_xz, self.height_ref)
         out, cache = self.forward(x)
         dout = self.ops.empty(*out.shape)
         loss = torch.zeros(1, dtype=torch.float32, device=self.device)
@@ -351,7 +368,7 @@ class Surrogate:
     def predict(self, height, wind_xz):
         """Predicted height change, fp32 [n,h,w]."""
         torch = self.torch
-        x = self.ops.pack(height, wind_xz)
+        x = self.ops.pack(height, wind_xz, self.height_ref)
         out, _ = self.forward(x)
         n, h, wd, _ = out.shape
         ch0 = torch.empty((n, h, wd), dtype=torch.float32, device=self.device)

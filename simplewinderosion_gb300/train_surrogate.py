@@ -181,7 +181,8 @@ def main(argv=None):
     meta = {"size": a.size, "cycles": a.cycles, "particles_per_cycle": a.size * a.size, "train_runs": a.runs,
             "train_lanes": data_lanes, "eval_lanes": "default",
             "eval_runs": a.eval_runs, "steps": a.steps, "batch": a.batch, "crop": 256, "data_s": data_s,
-            "train_s": train_s, **{k: v for k, v in ev.items() if k != "per_run"}}
+            "train_s": train_s, "height_ref": model.height_ref,
+            **{k: v for k, v in ev.items() if k != "per_run"}}
     print(json.dumps(meta))
     out = Path(a.out)
     out.parent.mkdir(parents=True, exist_ok=True)

@@ -72,6 +72,24 @@ def test_elementwise_blocks(ops):
     hgt = rs.uniform(0, 0.6, (2, 8, 6)).astype(np.float32)
     wind = np.asarray([[0.6, 0.8], [-1.0, 0.0]], np.float32)
     close(host(ops.pack(torch.from_numpy(hgt).cuda(), torch.from_numpy(wind).cuda())), R.pack_input(hgt, wind))
+    shifted = (hgt - np.float32(3.0)).astype(np.float32)
+    close(host(ops.pack(torch.from_numpy(shifted).cuda(), torch.from_numpy(wind).cuda(), ref=0.35)),
+          R.pack_input(shifted, wind, ref=0.35))
+
+
+def test_prediction_does_not_depend_on_the_height_level():
+    """The erosion rules see heights only through differences; the
+    surrogate's input is centred on its reference level, so a terrain and the
+    same terrain 2.5 lower get the same predicted change (within the bf16
+    rounding of the centred input)."""
+    from simplewinderosion_gb300 import surrogate
+    m = surrogate.Surrogate(seed=8)
+    rs = np.random.RandomState(9)
+    h = rs.uniform(0, 0.6, (2, 32, 32)).astype(np.float32)
+    wind = torch.from_numpy(np.asarray([[0.6, 0.8], [-1.0, 0.0]], np.float32)).cuda()
+    a = m.predict(torch.from_numpy(h).cuda(), wind).cpu().numpy()
+    b = m.predict(torch.from_numpy((h - np.float32(2.5)).astype(np.float32)).cuda(), wind).cpu().numpy()
+    assert np.abs(a - b).max() <= 0.05 * np.abs(a).max() + 1e-4
 
 
 def _model_and_reference(seed=4):
