@@ -1,6 +1,6 @@
 """Check (c) at exactly the benchmarked configuration: the parallel GPU mode
 at 1024^2, 1,048,576 particles per cycle, int32 Q16.16 heights and the
-default particles in flight (cells/64 = 16,384), against the reference's own
+default particles in flight (cells/256 = 4,096), against the reference's own
 sequential World::erode (source/world.hpp:36-77).
 
 The reference side is the committed fixture tests/golden/stats_1024_plain.npz
