@@ -21,6 +21,7 @@
 #include <cstdint>
 
 #include "swe_kernels.h"
+#include "swe_nn_math.cuh"
 
 namespace swe {
 namespace {
@@ -282,10 +283,8 @@ __global__ void k_bias_grad(const bf16* __restrict__ dy, float* __restrict__ db,
   for (int c = threadIdx.x; c < cout; c += blockDim.x) atomicAdd(db + c, sdb[c]);
 }
 
-__device__ __forceinline__ float gelu(float v) { return 0.5f * v * (1.0f + erff(v * 0.70710678f)); }
-__device__ __forceinline__ float gelu_grad(float v) {
-  return 0.5f * (1.0f + erff(v * 0.70710678f)) + v * 0.39894228f * expf(-0.5f * v * v);
-}
+__device__ __forceinline__ float gelu(float v) { return gelu_as(v); }
+__device__ __forceinline__ float gelu_grad(float v) { return gelu_grad_as(v); }
 
 // The elementwise kernels move 8 bf16 values (16 bytes) per thread step;
 // counts and channel numbers are multiples of 8 (checked by the callers).

@@ -39,6 +39,7 @@
 #include <mutex>
 
 #include "swe_kernels.h"
+#include "swe_nn_math.cuh"
 
 namespace swe {
 namespace {
@@ -175,7 +176,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float gelu_erf(float v) { return 0.5f * v * (1.0f + erff(v * 0.70710678118654752f)); }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
@@ -231,8 +231,10 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
   volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
   volatile int* consumed = abort + 1;  // k-blocks whose data the MMA thread took
 
+  __shared__ __align__(16) float s_bias[256];  // the bias (zeros without one), read by the epilogue
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kblocks = 9 * g.chunks;
+  for (int i = threadIdx.x; i < g.nc; i += blockDim.x) s_bias[i] = bias ? bias[i] : 0.0f;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < g.stages; s++) {
@@ -354,29 +356,31 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
         for (int j = half; j < g.nc / 16; j += 2) {
           float v[16];
           tmem_ld16(acc + mt * g.col_stride + 16 * j, v);
-          if (bias) {
+          const float4* bq = reinterpret_cast<const float4*>(s_bias + 16 * j);
 #pragma unroll
-            for (int i = 0; i < 16; i++) v[i] += bias[16 * j + i];
+          for (int i = 0; i < 4; i++) {
+            const float4 b4 = bq[i];
+            v[4 * i] += b4.x;
+            v[4 * i + 1] += b4.y;
+            v[4 * i + 2] += b4.z;
+            v[4 * i + 3] += b4.w;
           }
-          uint4 o0, o1;
-          o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
-          o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
-          o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
-          o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
-          uint4* dst = reinterpret_cast<uint4*>(y + pix * g.nc + 16 * j);
-          dst[0] = o0;
-          dst[1] = o1;
-          if (act) {
-            // GELU of the bf16-rounded pre-activation, as the separate GELU pass computes it
+          uint32_t w[8];
 #pragma unroll
-            for (int i = 0; i < 16; i++) v[i] = gelu_erf(__bfloat162float(__float2bfloat16_rn(v[i])));
-            o0.x = pack_bf16(v[0], v[1]); o0.y = pack_bf16(v[2], v[3]);
-            o0.z = pack_bf16(v[4], v[5]); o0.w = pack_bf16(v[6], v[7]);
-            o1.x = pack_bf16(v[8], v[9]); o1.y = pack_bf16(v[10], v[11]);
-            o1.z = pack_bf16(v[12], v[13]); o1.w = pack_bf16(v[14], v[15]);
+          for (int i = 0; i < 8; i++) w[i] = pack_bf16(v[2 * i], v[2 * i + 1]);
+          uint4* dst = reinterpret_cast<uint4*>(y + pix * g.nc + 16 * j);
+          dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+          dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+          if (act) {
+            // GELU of the bf16-rounded pre-activation (the values just
+            // packed), as the separate GELU pass computes it
+            uint32_t a[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+              a[i] = pack_bf16(gelu_as(__uint_as_float(w[i] << 16)), gelu_as(__uint_as_float(w[i] & 0xFFFF0000u)));
             uint4* da = reinterpret_cast<uint4*>(act + pix * g.nc + 16 * j);
-            da[0] = o0;
-            da[1] = o1;
+            da[0] = make_uint4(a[0], a[1], a[2], a[3]);
+            da[1] = make_uint4(a[4], a[5], a[6], a[7]);
           }
         }
       }

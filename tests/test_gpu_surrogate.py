@@ -77,6 +77,28 @@ def test_elementwise_blocks(ops):
           R.pack_input(shifted, wind, ref=0.35))
 
 
+def test_gelu_and_its_derivative_over_every_bf16_input(ops):
+    """The device GELU (Abramowitz & Stegun 7.1.26 for the normal CDF) on
+    every bf16 value in [-12, 12] against the exact erf form in float64: the
+    bf16 result is within one bf16 step of the exact value (or 1e-6 of it
+    where the value underflows), and so is the derivative path."""
+    import math
+    bits = np.arange(0, 1 << 16, dtype=np.uint32).astype(np.uint16)
+    v = (bits.astype(np.uint32) << 16).view(np.float32)
+    v = v[np.isfinite(v) & (np.abs(v) <= 12.0)]
+    v = v[: len(v) // 8 * 8].astype(np.float32)
+    erf = np.vectorize(math.erf)
+    exact = 0.5 * v.astype(np.float64) * (1.0 + erf(v.astype(np.float64) / math.sqrt(2.0)))
+    got = host(ops.gelu(dev(v.reshape(-1, 8)))).reshape(-1).astype(np.float64)
+    step = np.maximum(np.abs(exact) * 2.0 ** -7, 1e-6)
+    assert np.all(np.abs(got - exact) <= step), float(np.max(np.abs(got - exact) / step))
+    ones = np.ones_like(v)
+    dexact = 0.5 * (1.0 + erf(v.astype(np.float64) / math.sqrt(2.0))) + v * np.exp(-0.5 * v.astype(np.float64) ** 2) / math.sqrt(2 * math.pi)
+    dgot = host(ops.gelu_bwd(dev(v.reshape(-1, 8)), dev(ones.reshape(-1, 8)))).reshape(-1).astype(np.float64)
+    dstep = np.maximum(np.abs(dexact) * 2.0 ** -7, 1e-6)
+    assert np.all(np.abs(dgot - dexact) <= dstep), float(np.max(np.abs(dgot - dexact) / dstep))
+
+
 def test_prediction_does_not_depend_on_the_height_level():
     """The erosion rules see heights only through differences; the
     surrogate's input is centred on its reference level, so a terrain and the
