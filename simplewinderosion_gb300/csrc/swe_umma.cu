@@ -4,16 +4,18 @@
 // multi-stage mbarrier pipeline.
 //
 //   k_conv_tc   3x3 convolution, zero padding, NHWC bf16, as an implicit
-//               GEMM: rows = 128-pixel tiles of the output (two per CTA),
-//               columns = output channels, K = 9 taps x input channels.
-//               Per k-block (one tap, KC = 64, 32 or 16 input channels) the
-//               TMA loads the tap-shifted 128-pixel tile of the input
-//               straight from the NHWC tensor (pixels beyond the map edge
-//               arrive as zeros: the padding costs nothing) and the weight
-//               slice straight from the [n][tap][k] weights. One thread
-//               issues the copies, one the MMAs; all four warps run the
-//               epilogue (TMEM -> registers, + bias, optional fused GELU,
-//               bf16 stores). The input gradient is the same kernel on the
+//               GEMM: rows = 128-pixel tiles of the output (taken two at a
+//               time), columns = output channels, K = 9 taps x input
+//               channels. Persistent: up to three CTAs per SM stride over
+//               the tile pairs. Per k-block (one tap, KC = 64, 32 or 16
+//               input channels) the TMA loads the tap-shifted 128-pixel tile
+//               of the input straight from the NHWC tensor (pixels beyond
+//               the map edge arrive as zeros: the padding costs nothing) and
+//               the weight slice straight from the [n][tap][k] weights. One
+//               thread issues the copies, one the MMAs into one of two TMEM
+//               accumulator sets; four warps run the epilogue of the other
+//               set (TMEM -> registers, + bias, optional fused GELU, bf16
+//               stores). The input gradient is the same kernel on the
 //               output gradient with the weights flipped and transposed.
 //               Its operands sit in shared memory in the canonical K-major
 //               swizzled layout: one row of KC channels (128, 64 or 32
@@ -22,10 +24,10 @@
 //               full rows keep every L2 sector access whole.
 //   k_wgrad_tc  the weight gradient: per tap a GEMM with M = output
 //               channels, N = input channels, K = pixels, both operands
-//               MN-major in the canonical layout without swizzle: a TMA box
-//               of 8 channels x 128 pixels is 16 core matrices (8 x 16 bytes)
-//               along K (LBO = 128 bytes), the next 8 channels one box
-//               further on (SBO = 2048 bytes).
+//               MN-major in the canonical swizzled layout: a TMA box of MA
+//               channels x the tile's 128 pixels, the next MA channels one
+//               box further on; one dy tile per k-block serves up to nine
+//               tap-shifted x tiles.
 //
 // Every wait on an mbarrier is bounded (2 s by the global timer): past it the
 // kernel records an error code in g_tc_error, stops issuing work, waits
@@ -201,12 +203,14 @@ struct TcConvGeom {
   uint32_t swz;    // descriptor layout code of the swizzle
 };
 
-// warp 0 copies, warp 1 issues the MMAs, warps 2-9 run the epilogue: two
-// warps per TMEM lane quarter (warp w may read lanes 32 (w % 4) .. + 31),
-// each taking every other 16-column chunk, so that every SM sub-partition
-// issues the epilogue's conversions from two warps
-constexpr int kConvWarps = 10;
+// warp 0 copies, warp 1 issues the MMAs, warps 2-5 run the epilogue (warp w
+// may read TMEM lanes 32 (w % 4) .. + 31). Up to three CTAs share an SM
+// (each its own copy/MMA pipeline): with one CTA per SM the copies of a
+// tile's nine tap-shifted boxes, issued one after another by one thread,
+// set the pace.
+constexpr int kConvWarps = 6;
 constexpr int kConvEpilogueWarps = kConvWarps - 2;
+constexpr int kConvMaxCtasPerSm = 3;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -216,7 +220,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // blockIdx.x + gridDim.x, ...; the copies and MMAs run ahead through the
 // units' k-blocks in one stage ring while the epilogue warps drain the
 // previous unit's accumulators from the other TMEM set.
-__global__ void __launch_bounds__(kConvWarps * 32, 1)
+__global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
     k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap wmap,
               const float* __restrict__ bias, bf16* __restrict__ y, bf16* __restrict__ act, const TcConvGeom g) {
   extern __shared__ unsigned char smem_raw[];
@@ -337,9 +341,10 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
       mbar_wait(drain, 0u, abort, false, 6u);
     }
   } else {
-    // ---- epilogue: warps 2-9; warp w reads TMEM lanes 32 (w % 4) .. + 31,
-    // chunks j = (w - 2) / 4, + 2, ...
+    // ---- epilogue: warps 2-5; warp w reads TMEM lanes 32 (w % 4) .. + 31
+    // (with more epilogue warps, kPerQuarter share a quarter's chunks)
     const int q4 = warp & 3, l = q4 * 32 + lane, half = (warp - 2) >> 2;
+    constexpr int kPerQuarter = kConvEpilogueWarps / 4;  // warps per TMEM lane quarter
     int it = 0;
     for (int u = blockIdx.x; u < g.pairs; u += gridDim.x, it++) {
       const int tile0 = u * kTcMTiles, mt_n = min(kTcMTiles, g.tiles - tile0);
@@ -353,7 +358,7 @@ __global__ void __launch_bounds__(kConvWarps * 32, 1)
         const int t = tile0 + mt, qq = t % tiles_per_img;
         const long pix = ((long)(t / tiles_per_img) * g.H + (qq / (g.W / g.TW)) * g.R + l / g.TW) * g.W +
                          (qq % (g.W / g.TW)) * g.TW + l % g.TW;
-        for (int j = half; j < g.nc / 16; j += 2) {
+        for (int j = half; j < g.nc / 16; j += kPerQuarter) {
           float v[16];
           tmem_ld16(acc + mt * g.col_stride + 16 * j, v);
           const float4* bq = reinterpret_cast<const float4*>(s_bias + 16 * j);
@@ -635,11 +640,26 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   g.b_bytes = nc * g.KC * 2;
   g.stage_bytes = (kTcMTiles * g.a_tile + g.b_bytes + 1023) / 1024 * 1024;
   g.swz = g.KC == 64 ? 2u : (g.KC == 32 ? 4u : 6u);
-  g.stages = 6;
-  while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + 256 > 200 * 1024) g.stages--;
-  // At least 120 KiB, so that one CTA holds an SM (its TMEM allocation may be all 512 columns).
+  // CTAs per SM: the most (up to three) whose TMEM allocations fit in the
+  // SM's 512 columns and whose stage rings (at least three stages each, or
+  // two for one CTA) fit in its 228 KiB of shared memory (less 2 KiB per CTA
+  // for the static bias array and the system's reservation)
+  int cps = 1;
+  g.stages = 2;
+  for (int c = kConvMaxCtasPerSm; c >= 1; c--) {
+    if (c * g.ncols > 512) continue;
+    const size_t budget = (size_t)228 * 1024 / c - 2048;
+    int st = 6;
+    while (st > 2 && 1024 + (size_t)st * g.stage_bytes + 256 > budget) st--;
+    if (1024 + (size_t)st * g.stage_bytes + 256 > budget || (c > 1 && st < 3)) continue;
+    cps = c;
+    g.stages = st;
+    break;
+  }
   size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + 256;
-  if (smem < 120 * 1024) smem = 120 * 1024;
+  // at most cps CTAs on an SM (each holds TMEM): more than 1/(cps+1) of its shared memory each
+  const size_t floor_smem = (size_t)228 * 1024 / (cps + 1) + 1;
+  if (smem < floor_smem) smem = floor_smem;
   if (smem > 227 * 1024) return cudaErrorNotSupported;
 
   CUtensorMap xm, wm;
@@ -657,7 +677,8 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = g.pairs < sms ? g.pairs : (sms > 0 ? sms : 1);
+  const int slots = cps * (sms > 0 ? sms : 1);
+  const int grid = g.pairs < slots ? g.pairs : slots;
   k_conv_tc<<<grid, kConvWarps * 32, smem, s>>>(xm, wm, bias, static_cast<bf16*>(y), static_cast<bf16*>(act), g);
   return cudaGetLastError();
 }
@@ -683,26 +704,47 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   g.swzB = g.MB == 64 ? 2u : (g.MB == 32 ? 4u : 6u);
   g.tiles = (int)((long)N * H * W / 128);
   g.col_stride = (cin + 31) / 32 * 32;
-  g.taps = 9 * g.col_stride <= 512 ? 9 : 3;
-  int cols = 32;
-  while (cols < g.taps * g.col_stride) cols <<= 1;
-  g.ncols = cols;
   g.a_bytes = 256 * cout;  // 8 K steps x 16 pixels x cout x 2 bytes
-  // the most taps per k-block (9, 3 or 1, dividing the CTA's taps) with which two stages fit
   auto stage_of = [&](int kt) { return g.a_bytes + 256 * kt * cin; };
   // the MMA reads 128 rows of A (128 / MA blocks of 256 MA bytes = 32 KiB from
   // the stage's start): keep the last stage's reads inside the allocation
   auto tail_of = [&](int kt) { return stage_of(kt) < 32768 ? 32768 - stage_of(kt) : 0; };
-  g.kt = g.taps;
-  while (g.kt > 1 && 1024 + 2 * (size_t)stage_of(g.kt) + tail_of(g.kt) + 128 > 200 * 1024) g.kt /= 3;
+  // The shape, in order of preference: the most CTAs per SM (up to three,
+  // each its own copy/MMA pipeline), then the most taps per CTA (9 or 3:
+  // TMEM columns), then the most taps per k-block (9, 3 or 1: one dy tile for
+  // kt x tiles), with at least two stages in the CTA's share of the SM's
+  // 228 KiB of shared memory.
+  int cps = 0;
+  for (int c = 3; c >= 1 && !cps; c--) {
+    const size_t budget = (size_t)228 * 1024 / c - 1024;
+    for (int taps = 9; taps >= 3 && !cps; taps /= 3) {
+      if (taps * g.col_stride > 512) continue;
+      int cols = 32;
+      while (cols < taps * g.col_stride) cols <<= 1;
+      if (c * cols > 512) continue;
+      for (int kt = taps; kt >= 1 && !cps; kt /= 3) {
+        int st = 4;
+        while (st > 2 && 1024 + (size_t)st * stage_of(kt) + tail_of(kt) + 128 > budget) st--;
+        if (1024 + (size_t)st * stage_of(kt) + tail_of(kt) + 128 > budget) continue;
+        cps = c;
+        g.taps = taps;
+        g.ncols = cols;
+        g.kt = kt;
+        g.stages = st;
+      }
+    }
+  }
+  if (!cps) return cudaErrorNotSupported;
   g.stage_bytes = stage_of(g.kt);
   g.tail = tail_of(g.kt);
-  g.stages = 4;
-  while (g.stages > 2 && 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128 > 200 * 1024) g.stages--;
-  const size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;
-  // about two CTAs per SM in all, each summing a run of pixel tiles
+  size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;
+  // at most cps CTAs on an SM (each holds TMEM): more than 1/(cps+1) of its shared memory each
+  const size_t floor_smem = (size_t)228 * 1024 / (cps + 1) + 1;
+  if (smem < floor_smem) smem = floor_smem;
+  if (smem > 227 * 1024) return cudaErrorNotSupported;
+  // one wave: cps CTAs per SM in all, each summing a run of pixel tiles
   const int groups = 9 / g.taps;
-  int ctas_x = (2 * (sms > 0 ? sms : 148)) / groups;
+  int ctas_x = (cps * (sms > 0 ? sms : 148)) / groups;
   if (ctas_x < 1) ctas_x = 1;
   if (ctas_x > g.tiles) ctas_x = g.tiles;
   g.tiles_per_cta = (g.tiles + ctas_x - 1) / ctas_x;
