@@ -632,30 +632,32 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   g.pairs = (g.tiles + kTcMTiles - 1) / kTcMTiles;
   g.col_stride = 32;  // a power of two: every accumulator starts on a multiple of its width
   while (g.col_stride < nc) g.col_stride <<= 1;
-  g.nbuf = 2 * kTcMTiles * g.col_stride <= 512 ? 2 : 1;
-  int cols = 32;
-  while (cols < g.nbuf * kTcMTiles * g.col_stride) cols <<= 1;
-  g.ncols = cols;
   g.a_tile = 128 * g.KC * 2;
   g.b_bytes = nc * g.KC * 2;
   g.stage_bytes = (kTcMTiles * g.a_tile + g.b_bytes + 1023) / 1024 * 1024;
   g.swz = g.KC == 64 ? 2u : (g.KC == 32 ? 4u : 6u);
-  // CTAs per SM: the most (up to three) whose TMEM allocations fit in the
-  // SM's 512 columns and whose stage rings (at least three stages each, or
-  // two for one CTA) fit in its 228 KiB of shared memory (less 2 KiB per CTA
-  // for the static bias array and the system's reservation)
-  int cps = 1;
-  g.stages = 2;
-  for (int c = kConvMaxCtasPerSm; c >= 1; c--) {
-    if (c * g.ncols > 512) continue;
+  // CTAs per SM and TMEM accumulator sets: the most CTAs (up to three),
+  // then two sets rather than one, whose TMEM allocations fit in the SM's
+  // 512 columns and whose stage rings (at least two stages each) fit in its
+  // 228 KiB of shared memory (less 2 KiB per CTA for the static bias array
+  // and the system's reservation)
+  int cps = 0;
+  for (int c = kConvMaxCtasPerSm; c >= 1 && !cps; c--) {
     const size_t budget = (size_t)228 * 1024 / c - 2048;
     int st = 6;
     while (st > 2 && 1024 + (size_t)st * g.stage_bytes + 256 > budget) st--;
-    if (1024 + (size_t)st * g.stage_bytes + 256 > budget || (c > 1 && st < 3)) continue;
-    cps = c;
-    g.stages = st;
-    break;
+    if (1024 + (size_t)st * g.stage_bytes + 256 > budget) continue;
+    for (int nb = 2; nb >= 1 && !cps; nb--) {
+      int cols = 32;
+      while (cols < nb * kTcMTiles * g.col_stride) cols <<= 1;
+      if (cols > 512 || c * cols > 512) continue;
+      cps = c;
+      g.nbuf = nb;
+      g.ncols = cols;
+      g.stages = st;
+    }
   }
+  if (!cps) return cudaErrorNotSupported;
   size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + 256;
   // at most cps CTAs on an SM (each holds TMEM): more than 1/(cps+1) of its shared memory each
   const size_t floor_smem = (size_t)228 * 1024 / (cps + 1) + 1;
