@@ -426,32 +426,52 @@ __global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf
 // Network input, 16 channels per pixel: (height - 0.25) * 4, the wind
 // direction's x and z components, zeros.
 // With means (per map, device), the heights are first moved so that each
-// map's mean is `ref`: ((h - mean) + (ref - 0.25)) * 4.
+// map's mean is `ref`: ((h - mean) + (ref - 0.25)) * 4. A pixel's 16
+// channels (32 bytes) leave in two 16-byte stores where x is 16-byte aligned.
 __global__ void k_pack_input(const float* __restrict__ h, const float* __restrict__ wind_xz, bf16* __restrict__ x,
-                             int N, int H, int W, const float* __restrict__ means, float ref) {
+                             int N, int H, int W, const float* __restrict__ means, float ref, bool vec) {
   const long n = (long)N * H * W;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
     const long b = p / ((long)H * W);
+    const bf16 c0 = __float2bfloat16_rn(means ? ((h[p] - means[b]) + (ref - 0.25f)) * 4.0f : (h[p] - 0.25f) * 4.0f);
+    const bf16 c1 = __float2bfloat16_rn(wind_xz[2 * b]);
+    const bf16 c2 = __float2bfloat16_rn(wind_xz[2 * b + 1]);
     bf16* o = x + p * 16;
-    o[0] = __float2bfloat16_rn(means ? ((h[p] - means[b]) + (ref - 0.25f)) * 4.0f : (h[p] - 0.25f) * 4.0f);
-    o[1] = __float2bfloat16_rn(wind_xz[2 * b]);
-    o[2] = __float2bfloat16_rn(wind_xz[2 * b + 1]);
+    if (vec) {
+      const uint32_t w0 = (uint32_t)__bfloat16_as_ushort(c0) | ((uint32_t)__bfloat16_as_ushort(c1) << 16);
+      const uint32_t w1 = (uint32_t)__bfloat16_as_ushort(c2);
+      reinterpret_cast<uint4*>(o)[0] = make_uint4(w0, w1, 0u, 0u);
+      reinterpret_cast<uint4*>(o)[1] = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+      o[0] = c0;
+      o[1] = c1;
+      o[2] = c2;
 #pragma unroll
-    for (int c = 3; c < 16; c++) o[c] = __float2bfloat16_rn(0.0f);
+      for (int c = 3; c < 16; c++) o[c] = __float2bfloat16_rn(0.0f);
+    }
   }
 }
 
 // Squared-error loss on channel 0 of pred (C channels) against target *
 // tscale: sum of squares into *loss, d pred = 2 (pred - target tscale)
 // gscale on channel 0, zero elsewhere.
+// With vec (C a multiple of 8, dpred 16-byte aligned) a pixel's gradient
+// leaves in C / 8 16-byte stores.
 __global__ void k_mse(const bf16* __restrict__ pred, const float* __restrict__ target, float tscale,
-                      bf16* __restrict__ dpred, float* __restrict__ loss, long M, int C, float scale) {
+                      bf16* __restrict__ dpred, float* __restrict__ loss, long M, int C, float scale, bool vec) {
   float s = 0.0f;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < M; p += (long)gridDim.x * blockDim.x) {
     const float e = __bfloat162float(pred[p * C]) - target[p] * tscale;
     s += e * e;
-    dpred[p * C] = __float2bfloat16_rn(2.0f * e * scale);
-    for (int c = 1; c < C; c++) dpred[p * C + c] = __float2bfloat16_rn(0.0f);
+    const bf16 d0 = __float2bfloat16_rn(2.0f * e * scale);
+    if (vec) {
+      uint4* o = reinterpret_cast<uint4*>(dpred + p * C);
+      o[0] = make_uint4((uint32_t)__bfloat16_as_ushort(d0), 0u, 0u, 0u);
+      for (int c = 1; c < C / 8; c++) o[c] = make_uint4(0u, 0u, 0u, 0u);
+    } else {
+      dpred[p * C] = d0;
+      for (int c = 1; c < C; c++) dpred[p * C + c] = __float2bfloat16_rn(0.0f);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
@@ -614,14 +634,16 @@ __global__ void __launch_bounds__(1024) k_map_mean(const float* __restrict__ h, 
 cudaError_t nn_pack_input(const float* h, const float* wind_xz, void* x, int N, int H, int W, cudaStream_t s,
                           float* means, float ref) {
   if (means) k_map_mean<<<N, 1024, 0, s>>>(h, (long)H * W, means);
-  k_pack_input<<<grid_for((long)N * H * W), 256, 0, s>>>(h, wind_xz, static_cast<bf16*>(x), N, H, W, means, ref);
+  const bool vec = (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+  k_pack_input<<<grid_for((long)N * H * W), 256, 0, s>>>(h, wind_xz, static_cast<bf16*>(x), N, H, W, means, ref, vec);
   return cudaGetLastError();
 }
 
 cudaError_t nn_mse(const void* pred, const float* target, float tscale, void* dpred, float* loss, long M, int C,
                    float gscale, cudaStream_t s) {
+  const bool vec = C % 8 == 0 && (reinterpret_cast<uintptr_t>(dpred) & 15) == 0;
   k_mse<<<grid_for(M), 256, 0, s>>>(static_cast<const bf16*>(pred), target, tscale, static_cast<bf16*>(dpred), loss,
-                                    M, C, gscale);
+                                    M, C, gscale, vec);
   return cudaGetLastError();
 }
 
