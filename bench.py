@@ -362,7 +362,9 @@ def run_ours(args):
     tuned = w.tune(particles) if not args.no_tune and args.lanes >= 0 else None
     if tuned:
         form = {0: kernel_name, 1: "k_par_lanes (one 16-CTA cluster)",
-                2: f"k_par_lanes (cooperative grid of {tuned['ctas']} CTAs)"}[tuned["kind"]]
+                2: f"k_par_lanes (cooperative grid of {tuned['ctas']} CTAs)",
+                3: f"k_par_lanes (cooperative grid of {tuned['ctas']} CTAs of 128 threads, lanes spread over "
+                   f"the warps)"}.get(tuned["kind"], kernel_name)
         kernel_name = form if not (tuned["kind"] == 0) else kernel_name
     stream = torch.cuda.ExternalStream(w.stream(), device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)

@@ -172,12 +172,15 @@ int swe_world_set_cycle(swe_world* w, uint64_t cycle);
 /* Launch form of the PARALLEL kernel for a bounded number of particles in
  * flight: kind 0 = the default rule (one 16-CTA thread-block cluster up to
  * 4,096 lanes, else one CTA per SM), 1 = one cluster (up to 16,384 lanes),
- * 2 = a cooperative grid of `ctas` CTAs (0: one per SM; at most 2 per SM).
+ * 2 = a cooperative grid of `ctas` CTAs (0: one per SM; at most 4 per SM),
+ * 3 = the same with 128 threads per CTA and the CTA's lanes spread over its
+ * four warps (for at most 96 lanes per CTA; more take the packed grid).
  * The form changes no result, only speed; a form that cannot hold the lanes
  * falls back to the default. swe_world_tune is the autotuner: it times one
  * cycle of `particles` particles in each candidate form (default, cluster,
- * grids of 2 CTAs per SM, of one per SM, and of 3/4, 1/2 and 1/4 of the
- * SMs) on a scratch copy of the world (its size,
+ * grids of one per SM, of 3/4, 1/2 and 1/4 of the SMs, and of 2, 3 and 4
+ * CTAs per SM, spread grids of 1 and 2 CTAs per SM) on a scratch copy of
+ * the world (its size,
  * parameters, seed and heights; the world itself is not touched), keeps the
  * fastest for the world, caches it for the process per (size, particles,
  * lanes), and reports it with its time and the default form's time (0 when

@@ -388,7 +388,8 @@ class World:
 
     def set_form(self, kind: int, ctas: int = 0) -> None:
         """Launch form of the PARALLEL kernel (0 default, 1 one cluster, 2 a
-        grid of `ctas` CTAs); changes no result."""
+        grid of `ctas` CTAs, 3 the same with a CTA's lanes spread over four
+        warps); changes no result."""
         _check(lib.swe_world_set_form(self._h, int(kind), int(ctas)))
 
     def form(self) -> tuple[int, int]:

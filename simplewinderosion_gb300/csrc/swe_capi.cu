@@ -456,7 +456,7 @@ int swe_world_set_wait_limit(swe_world* w, uint64_t ns) {
 
 int swe_world_set_form(swe_world* w, int kind, int ctas) {
   if (!w) return fail(SWE_ERR_INVALID, "NULL world");
-  if (kind < 0 || kind > 2 || ctas < 0) return fail(SWE_ERR_INVALID, "kind must be 0, 1 or 2 and ctas >= 0");
+  if (kind < 0 || kind > 3 || ctas < 0) return fail(SWE_ERR_INVALID, "kind must be 0, 1, 2 or 3 and ctas >= 0");
   w->form.kind = kind;
   w->form.ctas = ctas;
   return SWE_OK;
@@ -511,7 +511,8 @@ int swe_world_tune(swe_world* w, int particles, int* kind, int* ctas, double* be
   cands.push_back(swe::LaunchForm{1, 0});
   for (int div : {1, 2, 4}) cands.push_back(swe::LaunchForm{2, sms / div > 0 ? sms / div : 1});
   cands.push_back(swe::LaunchForm{2, 3 * sms / 4 > 0 ? 3 * sms / 4 : 1});
-  cands.push_back(swe::LaunchForm{2, 2 * sms});  // two CTAs per SM, where they fit
+  for (int per = 2; per <= 4; per++) cands.push_back(swe::LaunchForm{2, per * sms});  // where they fit
+  for (int per = 1; per <= 2; per++) cands.push_back(swe::LaunchForm{3, per * sms});  // lanes spread over 4 warps
   double best = -1.0;
   swe::LaunchForm best_form;
   for (size_t i = 0; i <= cands.size(); i++) {

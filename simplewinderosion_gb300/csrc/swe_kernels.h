@@ -74,8 +74,11 @@ void launch_height_to_fixed(const float* height, int32_t* q, const Consts& c, Co
 int cycle_grid(int device);
 // Launch form of a bounded-lanes cycle: kind 0 the default rule (one 16-CTA
 // cluster up to 4,096 lanes, else one CTA per SM), 1 one cluster (up to
-// 16,384 lanes), 2 a cooperative grid of `ctas` CTAs (0: one per SM). The
-// form changes no result: only the set of particles in flight matters.
+// 16,384 lanes), 2 a cooperative grid of `ctas` CTAs (0: one per SM), 3 the
+// same with 128 threads per CTA and the CTA's lanes spread over its four
+// warps (fewer lanes per warp, so a warp's polling loops wait on fewer
+// cells). The form changes no result: only the set of particles in flight
+// matters.
 struct LaunchForm {
   int kind = 0;
   int ctas = 0;

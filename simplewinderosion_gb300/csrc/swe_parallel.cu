@@ -221,6 +221,7 @@ struct CycleArgs {
   GridBarrier* gb;
   int particles;  // particles of the cycle
   int lanes;      // particles in flight at once
+  int spread;     // bounded lanes: a CTA's lanes spread over its warps (lane l of warp w first) instead of packed
 };
 
 // Per-thread tallies of the colour phases.
@@ -1103,9 +1104,10 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
   const int L = A.lanes;
   const int Lr = L / nb + ((int)r < L % nb ? 1 : 0);
   unsigned lanes_mask = 0;
+  const int order = A.spread ? lane * nwarps + warp : t;  // this thread's place in the CTA's lane order
 #pragma unroll
   for (int s = 0; s < kClusterMaxSlots; s++)
-    if (s < slots && s * T + t < Lr) lanes_mask |= 1u << s;
+    if (s < slots && s * T + order < Lr) lanes_mask |= 1u << s;
   unsigned live = 0;
   const int lane_id0 = (int)r * cap;  // lane slot j of this CTA has id lane_id0 + j
 
@@ -1812,6 +1814,7 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   A.gb = gb;
   A.particles = particles;
   A.lanes = lanes;
+  A.spread = 0;
   const long n = (long)c.nx * c.nz;
   // Bounded lanes: one cluster, or one CTA per SM; cell indices are 32-bit there.
   int sms = 0, dev = 0;
@@ -1825,15 +1828,21 @@ cudaError_t launch_par_cycle(const ParallelBuffers& B, const Fields& F, const Co
   int ctas = sms;
   if (form.kind == 1 && lanes_shape(lanes, kClusterCtas, kClusterMaxThreads, &threads, &slots)) {
     cluster = true;
-  } else if (form.kind == 2) {
-    const int want = form.ctas > 0 && form.ctas <= 2 * sms ? form.ctas : sms;
+  } else if (form.kind == 2 || form.kind == 3) {
+    const int want = form.ctas > 0 && form.ctas <= 4 * sms ? form.ctas : sms;
     if (lanes_shape(lanes, want, kLanesGridMaxThreads, &threads, &slots)) {
       cluster = false;
       ctas = want;
+      A.spread = form.kind == 3 ? 1 : 0;
     }
   }
   if (n <= (1l << 30) && lanes_shape(lanes, cluster ? kClusterCtas : ctas,
                                      cluster ? kClusterMaxThreads : kLanesGridMaxThreads, &threads, &slots)) {
+    if (A.spread && threads < 128) {
+      // four warps share the CTA's lanes (at most 96 of them here: one slot each)
+      threads = 128;
+      slots = 1;
+    }
     k_cluster_prologue<<<sweep_grid(n), 256, 0, s>>>(B, n);
     bool launched = false;
     const cudaError_t e = cluster ? launch_cluster(A, threads, slots, s, &launched)
@@ -1903,6 +1912,7 @@ cudaError_t upload_batch_items(const BatchWorld* worlds, int count, const BatchS
     A.gb = w.gb;
     A.particles = w.particles;
     A.lanes = w.lanes;
+    A.spread = 0;
     int threads = 0, slots = 0;
     if ((long)w.c.nx * w.c.nz > (1l << 30) || !lanes_shape(w.lanes, sh.ctas, sh.threads, &threads, &slots))
       return cudaErrorInvalidValue;

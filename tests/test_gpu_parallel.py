@@ -145,7 +145,8 @@ def test_upload_download_roundtrip_every_field():
         w.upload(swe.Field.HEIGHT, np.zeros(10, np.float32))
 
 
-@pytest.mark.parametrize("kind,ctas", [(1, 0), (2, 0), (2, 38), (2, 76), (2, 114), (2, 304)])
+@pytest.mark.parametrize("kind,ctas", [(1, 0), (2, 0), (2, 38), (2, 76), (2, 114), (2, 304), (2, 456), (2, 608),
+                                       (3, 0), (3, 152), (3, 304)])
 def test_launch_forms_give_the_same_result(kind, ctas):
     """Every launch form of the bounded-lanes kernel (one cluster, grids of
     various CTA counts) leaves the world bit for bit as the CPU model does."""
