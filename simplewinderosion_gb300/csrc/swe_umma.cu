@@ -191,13 +191,21 @@ struct TcConvGeom {
   int TW, R;   // an M tile: R image rows x TW pixels = 128 pixels
   int KC;      // channels per k-block: 64, 32 or 16, one swizzled row of 128, 64 or 32 bytes per pixel
   int chunks;  // kc / KC
-  int tiles;   // 128-pixel tiles in the batch
-  int pairs;   // units of work: kTcMTiles consecutive tiles that share every weight slice
+  int vertical;  // 1: a unit is kTcMTiles vertically adjacent tiles and a k-block (dx, chunk) takes one
+                 // input box of the unit's rows and one row above and below, which serves the three dy
+                 // taps; 0: a unit is kTcMTiles consecutive tiles and a k-block (tap, chunk) takes one
+                 // tap-shifted box per tile
+  int tpr;       // tiles side by side in a row group (W / TW)
+  int rgroups;   // row groups of R image rows in a map (H / R)
+  int ublocks;   // vertical units stacked in a column of tiles (rgroups / kTcMTiles, rounded up)
+  int tiles;     // 128-pixel tiles in the batch
+  int units;     // units of work
+  int xrows;     // image rows of one input box: R kTcMTiles + 2 (vertical) or R
+  int x_bytes;   // bytes of the input boxes per k-block (kTcMTiles x 128 or xrows x TW rows of KC channels)
   int col_stride;  // TMEM columns between the M tiles of a unit
   int nbuf;        // TMEM accumulator sets (2: the epilogue of one unit overlaps the next unit's MMAs)
   int ncols;       // TMEM columns allocated
-  int a_tile;      // bytes of one M tile's operand per k-block (128 rows)
-  int b_bytes;     // bytes of the weight slice per k-block (nc rows)
+  int b_bytes;     // bytes of one tap's weight slice (nc rows of KC channels); three per k-block if vertical
   int stage_bytes;
   int stages;      // pipeline depth (2..6)
   uint32_t swz;    // descriptor layout code of the swizzle
@@ -209,6 +217,23 @@ struct TcConvGeom {
 // tile's nine tap-shifted boxes, issued one after another by one thread,
 // set the pace.
 constexpr int kConvWarps = 6;
+
+// Tile mt of unit u: its image n and top-left pixel (y, x); returns the
+// unit's tile count.
+__device__ __forceinline__ int unit_tile(const TcConvGeom& g, int u, int mt, int& n, int& y, int& x) {
+  if (g.vertical) {
+    const int upi = g.tpr * g.ublocks, q = u % upi, rg0 = (q / g.tpr) * kTcMTiles;
+    n = u / upi;
+    x = (q % g.tpr) * g.TW;
+    y = (rg0 + mt) * g.R;
+    return min(kTcMTiles, g.rgroups - rg0);
+  }
+  const int t = u * kTcMTiles + mt, tpi = g.tpr * g.rgroups, q = t % tpi;
+  n = t / tpi;
+  y = (q / g.tpr) * g.R;
+  x = (q % g.tpr) * g.TW;
+  return min(kTcMTiles, g.tiles - u * kTcMTiles);
+}
 constexpr int kConvEpilogueWarps = kConvWarps - 2;
 constexpr int kConvMaxCtasPerSm = 3;
 
@@ -237,7 +262,8 @@ __global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
 
   __shared__ __align__(16) float s_bias[256];  // the bias (zeros without one), read by the epilogue
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int kblocks = 9 * g.chunks;
+  const int kblocks = (g.vertical ? 3 : 9) * g.chunks;  // (dx, chunk) or (tap, chunk)
+  const int ntap = g.vertical ? 3 : 1;                   // taps per k-block
   for (int i = threadIdx.x; i < g.nc; i += blockDim.x) s_bias[i] = bias ? bias[i] : 0.0f;
 
   if (threadIdx.x == 0) {
@@ -264,24 +290,22 @@ __global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int tiles_per_img = (g.H * g.W) >> 7;
 
   int issued = 0;  // producer: k-blocks whose copies were issued
   if (warp == 0) {
     if (lane == 0) {
-      // ---- producer: one TMA box per M tile for the tap-shifted input, one for the weight slice
+      // ---- producer: per k-block (vertical) one box of the dx-shifted input
+      // covering the unit's rows and one row above and below and the three
+      // dy taps' weight slices, or (otherwise) one tap-shifted box per tile
+      // and the tap's weight slice; pixels past the map edge arrive as zeros
       int kbg = 0;
-      for (int u = blockIdx.x; u < g.pairs && !*abort; u += gridDim.x) {
-        const int tile0 = u * kTcMTiles, mt_n = min(kTcMTiles, g.tiles - tile0);
+      for (int u = blockIdx.x; u < g.units && !*abort; u += gridDim.x) {
         int tn[kTcMTiles], ty[kTcMTiles], tx[kTcMTiles];
+        int mt_n = 0;
 #pragma unroll
-        for (int mt = 0; mt < kTcMTiles; mt++) {
-          const int t = tile0 + mt, q = t % tiles_per_img;
-          tn[mt] = t / tiles_per_img;
-          ty[mt] = (q / (g.W / g.TW)) * g.R;
-          tx[mt] = (q % (g.W / g.TW)) * g.TW;
-        }
-        const uint32_t bytes = (uint32_t)mt_n * g.a_tile + g.b_bytes;
+        for (int mt = 0; mt < kTcMTiles; mt++) mt_n = unit_tile(g, u, mt, tn[mt], ty[mt], tx[mt]);
+        const uint32_t bytes = g.vertical ? (uint32_t)g.x_bytes + 3u * (uint32_t)g.b_bytes
+                                          : (uint32_t)(mt_n * 128 * 2 * g.KC + g.b_bytes);
         bool ok = true;
         for (int kb = 0; kb < kblocks; kb++, kbg++) {
           const int s = kbg % g.stages;
@@ -290,13 +314,19 @@ __global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
             ok = false;
             break;
           }
-          const int tap = kb / g.chunks, chunk = kb % g.chunks;
-          const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+          const int kq = kb / g.chunks, chunk = kb % g.chunks;  // kq: dx + 1 (vertical) or the tap
           unsigned char* st = smem + s * g.stage_bytes;
           mbar_expect_tx(full + s, bytes);
-          for (int mt = 0; mt < mt_n; mt++)
-            tma_load_4d(st + mt * g.a_tile, &xmap, full + s, chunk * g.KC, tx[mt] + dx, ty[mt] + dy, tn[mt]);
-          tma_load_3d(st + kTcMTiles * g.a_tile, &wmap, full + s, chunk * g.KC, tap, 0);
+          if (g.vertical) {
+            tma_load_4d(st, &xmap, full + s, chunk * g.KC, tx[0] + kq - 1, ty[0] - 1, tn[0]);
+            for (int dy = 0; dy < 3; dy++)
+              tma_load_3d(st + g.x_bytes + dy * g.b_bytes, &wmap, full + s, chunk * g.KC, dy * 3 + kq, 0);
+          } else {
+            const int dy = kq / 3 - 1, dx = kq % 3 - 1;
+            for (int mt = 0; mt < mt_n; mt++)
+              tma_load_4d(st + mt * 128 * 2 * g.KC, &xmap, full + s, chunk * g.KC, tx[mt] + dx, ty[mt] + dy, tn[mt]);
+            tma_load_3d(st + g.x_bytes, &wmap, full + s, chunk * g.KC, kq, 0);
+          }
           issued = kbg + 1;
         }
         if (!ok) break;
@@ -310,8 +340,10 @@ __global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
       const uint32_t sbo = 16u * (uint32_t)g.KC;  // 8 rows of KC bf16
       int kbg = 0, it = 0;
       bool ok = true;
-      for (int u = blockIdx.x; u < g.pairs && ok; u += gridDim.x, it++) {
-        const int mt_n = min(kTcMTiles, g.tiles - u * kTcMTiles);
+      const uint32_t row_bytes = 2u * (uint32_t)g.KC;
+      for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x, it++) {
+        int n0, y0, x0;
+        const int mt_n = unit_tile(g, u, 0, n0, y0, x0);
         const int b = it % g.nbuf, use = it / g.nbuf;
         if (!mbar_wait(tempty + b, (uint32_t)(use & 1) ^ 1u, abort, true, 5u)) break;
         tc_fence_after();
@@ -324,12 +356,18 @@ __global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
             break;
           }
           tc_fence_after();
-          const uint32_t a0 = sb + s * g.stage_bytes, b0 = a0 + kTcMTiles * g.a_tile;
+          const uint32_t x_base = sb + s * g.stage_bytes, w_base = x_base + g.x_bytes;
           for (int mt = 0; mt < mt_n; mt++) {
-            for (int j = 0; j < g.KC / 16; j++) {
-              const uint64_t ad = smem_desc_sw(a0 + mt * g.a_tile + 32 * j, sbo, g.swz);
-              const uint64_t bd = smem_desc_sw(b0 + 32 * j, sbo, g.swz);
-              umma_bf16(acc + mt * g.col_stride, ad, bd, idesc, (kb > 0 || j > 0) ? 1u : 0u);
+            for (int dy = 0; dy < ntap; dy++) {
+              // tile mt's 128 pixels (shifted by dy rows if vertical): box rows
+              // (mt R + dy) TW on, a whole number of 8-row swizzle atoms (TW >= 8)
+              const uint32_t a0 = x_base + (uint32_t)((mt * g.R + dy) * g.TW) * row_bytes;
+              const uint32_t b0 = w_base + (uint32_t)(dy * g.b_bytes);
+              for (int j = 0; j < g.KC / 16; j++) {
+                const uint64_t ad = smem_desc_sw(a0 + 32 * j, sbo, g.swz);
+                const uint64_t bd = smem_desc_sw(b0 + 32 * j, sbo, g.swz);
+                umma_bf16(acc + mt * g.col_stride, ad, bd, idesc, (kb > 0 || dy > 0 || j > 0) ? 1u : 0u);
+              }
             }
           }
           umma_commit(empty + s);  // the stage is free once these MMAs have read it
@@ -346,18 +384,20 @@ __global__ void __launch_bounds__(kConvWarps * 32, kConvMaxCtasPerSm)
     const int q4 = warp & 3, l = q4 * 32 + lane, half = (warp - 2) >> 2;
     constexpr int kPerQuarter = kConvEpilogueWarps / 4;  // warps per TMEM lane quarter
     int it = 0;
-    for (int u = blockIdx.x; u < g.pairs; u += gridDim.x, it++) {
-      const int tile0 = u * kTcMTiles, mt_n = min(kTcMTiles, g.tiles - tile0);
+    for (int u = blockIdx.x; u < g.units; u += gridDim.x, it++) {
+      int img0, row00, col00;
+      const int mt_n = unit_tile(g, u, 0, img0, row00, col00);
       const int b = it % g.nbuf, use = it / g.nbuf;
       const bool have = mbar_wait(tfull + b, (uint32_t)(use & 1), abort, true, 3u);
       tc_fence_after();
       if (!__all_sync(0xffffffffu, have && *abort == 0)) break;
       const uint32_t acc = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kTcMTiles * g.col_stride);
       for (int mt = 0; mt < mt_n; mt++) {
-        // TMEM lane l of the tile is image pixel (ty + l / TW, tx + l % TW)
-        const int t = tile0 + mt, qq = t % tiles_per_img;
-        const long pix = ((long)(t / tiles_per_img) * g.H + (qq / (g.W / g.TW)) * g.R + l / g.TW) * g.W +
-                         (qq % (g.W / g.TW)) * g.TW + l % g.TW;
+        // TMEM lane l of tile mt is image pixel (row0 + l / TW, col0 + l % TW)
+        // (names that do not hide the output pointer y)
+        int img, row0, col0;
+        unit_tile(g, u, mt, img, row0, col0);
+        const long pix = ((long)img * g.H + row0 + l / g.TW) * g.W + col0 + l % g.TW;
         for (int j = half; j < g.nc / 16; j += kPerQuarter) {
           float v[16];
           tmem_ld16(acc + mt * g.col_stride + 16 * j, v);
@@ -600,6 +640,9 @@ cudaError_t make_map(CUtensorMap* map, const void* t, int rank, const cuuint64_t
                      const cuuint32_t* box, int row_bytes) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
+  // every box fits inside its tensor (no dimension of a box exceeds the tensor's)
+  for (int i = 0; i < rank; i++)
+    if ((cuuint64_t)box[i] > dims[i]) return cudaErrorInvalidValue;
   const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   const CUtensorMapSwizzle sw = row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
                                 : row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
@@ -627,37 +670,65 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   g.R = 128 / g.TW;
   g.KC = kc % 64 == 0 ? 64 : (kc % 32 == 0 ? 32 : 16);
   g.chunks = kc / g.KC;
-  const long pixels = (long)N * H * W;
-  g.tiles = (int)(pixels / 128);
-  g.pairs = (g.tiles + kTcMTiles - 1) / kTcMTiles;
+  g.tpr = W / g.TW;
+  g.rgroups = H / g.R;
+  g.ublocks = (g.rgroups + kTcMTiles - 1) / kTcMTiles;
+  const long tiles = (long)N * g.tpr * g.rgroups;
+  const long vunits = (long)N * g.tpr * g.ublocks;
+  if (vunits > 0x7FFFFFFFl || tiles > 0x7FFFFFFFl) return cudaErrorNotSupported;
+  g.tiles = (int)tiles;
   g.col_stride = 32;  // a power of two: every accumulator starts on a multiple of its width
   while (g.col_stride < nc) g.col_stride <<= 1;
-  g.a_tile = 128 * g.KC * 2;
   g.b_bytes = nc * g.KC * 2;
-  g.stage_bytes = (kTcMTiles * g.a_tile + g.b_bytes + 1023) / 1024 * 1024;
   g.swz = g.KC == 64 ? 2u : (g.KC == 32 ? 4u : 6u);
-  // CTAs per SM and TMEM accumulator sets: the most CTAs (up to three),
-  // then two sets rather than one, whose TMEM allocations fit in the SM's
-  // 512 columns and whose stage rings (at least two stages each) fit in its
-  // 228 KiB of shared memory (less 2 KiB per CTA for the static bias array
-  // and the system's reservation)
-  int cps = 0;
-  for (int c = kConvMaxCtasPerSm; c >= 1 && !cps; c--) {
-    const size_t budget = (size_t)228 * 1024 / c - 2048;
-    int st = 6;
-    while (st > 2 && 1024 + (size_t)st * g.stage_bytes + 256 > budget) st--;
-    if (1024 + (size_t)st * g.stage_bytes + 256 > budget) continue;
-    for (int nb = 2; nb >= 1 && !cps; nb--) {
-      int cols = 32;
-      while (cols < nb * kTcMTiles * g.col_stride) cols <<= 1;
-      if (cols > 512 || c * cols > 512) continue;
-      cps = c;
-      g.nbuf = nb;
-      g.ncols = cols;
-      g.stages = st;
+  // The unit scheme and the launch shape. For each scheme: the most CTAs
+  // per SM (up to three), then two TMEM accumulator sets rather than one,
+  // whose TMEM allocations fit in the SM's 512 columns and whose stage rings
+  // (at least two stages each) fit in its 228 KiB of shared memory (less
+  // 2 KiB per CTA for the static bias array and the system's reservation).
+  // Then the scheme that copies fewer rows per unit and CTA: a unit's input
+  // rows, one per pixel and k-block, are what sets the pace.
+  struct Plan {
+    int cps = 0, nbuf = 0, ncols = 0, stages = 0, x_bytes = 0, stage_bytes = 0;
+    double cost = 0.0;
+  };
+  auto plan_for = [&](int vertical) {
+    Plan p;
+    const int xrows = vertical ? g.R * kTcMTiles + 2 : g.R;
+    p.x_bytes = vertical ? xrows * g.TW * g.KC * 2 : kTcMTiles * 128 * g.KC * 2;
+    p.stage_bytes = (p.x_bytes + (vertical ? 3 : 1) * g.b_bytes + 1023) / 1024 * 1024;
+    for (int c = kConvMaxCtasPerSm; c >= 1 && !p.cps; c--) {
+      const size_t budget = (size_t)228 * 1024 / c - 2048;
+      int st = 6;
+      while (st > 2 && 1024 + (size_t)st * p.stage_bytes + 256 > budget) st--;
+      if (1024 + (size_t)st * p.stage_bytes + 256 > budget) continue;
+      for (int nb = 2; nb >= 1 && !p.cps; nb--) {
+        int cols = 32;
+        while (cols < nb * kTcMTiles * g.col_stride) cols <<= 1;
+        if (cols > 512 || c * cols > 512) continue;
+        p.cps = c;
+        p.nbuf = nb;
+        p.ncols = cols;
+        p.stages = st;
+      }
     }
-  }
-  if (!cps) return cudaErrorNotSupported;
+    const double rows = vertical ? 3.0 * xrows * g.TW : 9.0 * kTcMTiles * 128;
+    p.cost = p.cps ? rows / p.cps : 1e30;
+    return p;
+  };
+  // the vertical scheme's input box (R kTcMTiles + 2 rows) must fit in the map's height
+  const Plan pv = g.R * kTcMTiles + 2 <= H ? plan_for(1) : Plan(), ph = plan_for(0);
+  if (!pv.cps && !ph.cps) return cudaErrorNotSupported;
+  g.vertical = pv.cps && (!ph.cps || pv.cost <= ph.cost) ? 1 : 0;
+  const Plan& pl = g.vertical ? pv : ph;
+  const int cps = pl.cps;
+  g.nbuf = pl.nbuf;
+  g.ncols = pl.ncols;
+  g.stages = pl.stages;
+  g.x_bytes = pl.x_bytes;
+  g.stage_bytes = pl.stage_bytes;
+  g.xrows = g.vertical ? g.R * kTcMTiles + 2 : g.R;
+  g.units = g.vertical ? (int)vunits : (int)((tiles + kTcMTiles - 1) / kTcMTiles);
   size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + 256;
   // at most cps CTAs on an SM (each holds TMEM): more than 1/(cps+1) of its shared memory each
   const size_t floor_smem = (size_t)228 * 1024 / (cps + 1) + 1;
@@ -667,7 +738,7 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   CUtensorMap xm, wm;
   const cuuint64_t xd[4] = {(cuuint64_t)kc, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
   const cuuint64_t xs[3] = {(cuuint64_t)kc * 2, (cuuint64_t)W * kc * 2, (cuuint64_t)H * W * kc * 2};
-  const cuuint32_t xb[4] = {(cuuint32_t)g.KC, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
+  const cuuint32_t xb[4] = {(cuuint32_t)g.KC, (cuuint32_t)g.TW, (cuuint32_t)g.xrows, 1};
   const cuuint64_t wd[3] = {(cuuint64_t)kc, 9, (cuuint64_t)nc};
   const cuuint64_t ws[2] = {(cuuint64_t)kc * 2, (cuuint64_t)9 * kc * 2};
   const cuuint32_t wb[3] = {(cuuint32_t)g.KC, 1, (cuuint32_t)nc};
@@ -680,7 +751,7 @@ cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int slots = cps * (sms > 0 ? sms : 1);
-  const int grid = g.pairs < slots ? g.pairs : slots;
+  const int grid = g.units < slots ? g.units : slots;
   k_conv_tc<<<grid, kConvWarps * 32, smem, s>>>(xm, wm, bias, static_cast<bf16*>(y), static_cast<bf16*>(act), g);
   return cudaGetLastError();
 }

@@ -65,10 +65,13 @@ def test_tc_conv_forward_and_input_gradient(ops, shape):
 @pytest.mark.parametrize("shape", [
     (8, 64, 256, 32, 96),   # 512 tile pairs: every CTA of the persistent grid takes 3-4, two accumulator sets
     (5, 64, 256, 16, 256),  # 320 pairs with 256 output channels: one accumulator set, reused in turn
+    (4, 64, 256, 64, 32),   # the tap-per-k-block scheme (64-channel rows) with several units per CTA
 ])
 def test_tc_conv_persistent_many_units(ops, shape):
-    """More units (pairs of 128-pixel tiles) than SMs: each CTA runs the
-    stage ring through several units and reuses its TMEM accumulator sets."""
+    """More units (pairs of 128-pixel tiles) than CTAs: each CTA runs the
+    stage ring through several units and reuses its TMEM accumulator sets;
+    both unit schemes (vertically adjacent tiles sharing one input box per
+    dx, and one tap-shifted box per tile and tap) are taken."""
     n, h, w, cin, cout = shape
     rs = np.random.RandomState(cin + cout)
     x = R.bf16(rs.standard_normal((n, h, w, cin)))
