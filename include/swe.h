@@ -409,7 +409,8 @@ int swe_nn_conv3x3_tc(const void* x, const void* wp, const float* bias, void* y,
 /* Weight and bias gradients of swe_nn_conv3x3 on the tensor cores, ADDED to
  * dw (fp32 [cout,3,3,cin]) and db (fp32 [cout], or NULL): per tap a GEMM
  * with M = output channels, N = input channels, K = pixels (split over
- * CTAs, partial sums added with fp32 atomics). cin and cout multiples of 16
+ * CTAs, partial sums added with fp32 atomics); the bias gradient in the same
+ * kernel, dy against a block of ones. cin and cout multiples of 16
  * up to 128; map shape as for swe_nn_conv3x3_tc; x and dy 16-byte aligned. */
 int swe_nn_conv3x3_wgrad_tc(const void* x, const void* dy, float* dw, float* db, int n, int h, int wd, int cin,
                             int cout, void* stream);

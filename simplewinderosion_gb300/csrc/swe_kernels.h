@@ -191,9 +191,10 @@ cudaError_t nn_pack_tc(const void* w, void* wp, int cin, int cout, bool flip, cu
 cudaError_t nn_conv_tc(const void* x, const void* wp, const float* bias, void* y, void* act, int N, int H, int W,
                        int kc, int nc, cudaStream_t s);
 bool nn_wgrad_tc_supported(int H, int W, int cin, int cout);
-// dw (fp32 [cout,3,3,cin]) += the weight gradient; sms: the device's SMs (sizes the split over pixels).
-cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, int W, int cin, int cout, int sms,
-                        cudaStream_t s);
+// dw (fp32 [cout,3,3,cin]) += the weight gradient, and db (fp32 [cout], or
+// nullptr) += the bias gradient; sms: the device's SMs (sizes the split over pixels).
+cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, float* db, int N, int H, int W, int cin, int cout,
+                        int sms, cudaStream_t s);
 // The first error code a tensor-core kernel recorded since the last call (0: none); clears it.
 cudaError_t nn_tc_status(unsigned int* code);
 

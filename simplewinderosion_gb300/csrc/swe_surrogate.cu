@@ -729,9 +729,7 @@ int swe_nn_conv3x3_wgrad_tc(const void* x, const void* dy, float* dw, float* db,
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return nn_fail(SWE_ERR_CUDA, "no current device");
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = swe::nn_wgrad_tc(x, dy, dw, n, h, wd, cin, cout, sms, s);
-  if (e == cudaSuccess && db) e = swe::nn_bias_grad(dy, db, (long)n * h * wd, cout, s);
-  return nn_done(e);
+  return nn_done(swe::nn_wgrad_tc(x, dy, dw, db, n, h, wd, cin, cout, sms, s));
 }
 
 int swe_nn_status(uint32_t* status) {

@@ -460,6 +460,7 @@ struct TcWgradGeom {
   int stages;
   int a_bytes, stage_bytes;
   int tail;  // bytes after the stages, so that the padded M rows of the last A operand stay in the allocation
+  int db_col;  // TMEM column of the bias-gradient accumulator (CTAs of tap group 0, with db), or -1
 };
 
 // Weight gradient dW[co][tap][ci] += sum over pixels p of dy[p][co] x[p + tap][ci]
@@ -475,11 +476,14 @@ struct TcWgradGeom {
 // partial sums leave TMEM through fp32 atomics into dw.
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap,
-               float* __restrict__ dw, const TcWgradGeom g) {
+               float* __restrict__ dw, float* __restrict__ db, const TcWgradGeom g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + g.stages * g.stage_bytes + g.tail);
+  // 16 channels x 128 pixels of bf16 ones (4 KiB, after the stages and the
+  // tail): the B operand of the bias gradient, db[co] = sum_p dy[p][co] x 1
+  unsigned char* ones = smem + (g.stages * g.stage_bytes + g.tail + 1023) / 1024 * 1024;
+  uint64_t* full = reinterpret_cast<uint64_t*>(ones + 4096);
   uint64_t* empty = full + 4;
   uint64_t* accum = empty + 4;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
@@ -492,6 +496,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int tap0 = blockIdx.y * g.taps;
   const int gk = g.taps / g.kt;  // k-blocks per tile
   const int kblocks = nt * gk;
+  const bool with_db = db != nullptr && blockIdx.y == 0 && g.db_col >= 0;
+  if (with_db) {
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) reinterpret_cast<uint32_t*>(ones)[i] = 0x3F803F80u;
+    // the MMAs read it through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < g.stages; s++) {
@@ -541,7 +551,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
   } else if (warp == 1 && lane == 0) {
     const uint32_t idesc = idesc_bf16_mn(128, g.cin);
-    const uint32_t sb = smem_u32(smem);
+    const uint32_t idesc16 = idesc_bf16_mn(128, 16);
+    const uint32_t sb = smem_u32(smem), so = smem_u32(ones);
     int kb = 0;
     for (; kb < kblocks; kb++) {
       const int s = kb % g.stages;
@@ -557,6 +568,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.MA, 256 * g.MA, 16 * g.MA, g.swzA);
           const uint64_t bd = smem_desc_full(b0 + k16 * 32 * g.MB, 256 * g.MB, 16 * g.MB, g.swzB);
           umma_bf16(tmem + (j0 + k) * g.col_stride, ad, bd, idesc, (i > 0 || k16 > 0) ? 1u : 0u);
+        }
+      }
+      if (with_db && j0 == 0) {
+        // once per pixel tile: dy against the ones (N = 16 identical columns)
+#pragma unroll
+        for (int k16 = 0; k16 < 8; k16++) {
+          const uint64_t ad = smem_desc_full(a0 + k16 * 32 * g.MA, 256 * g.MA, 16 * g.MA, g.swzA);
+          const uint64_t od = smem_desc_full(so + k16 * 32 * 16, 256 * 16, 16 * 16, 6u);
+          umma_bf16(tmem + (uint32_t)g.db_col, ad, od, idesc16, (i > 0 || k16 > 0) ? 1u : 0u);
         }
       }
       umma_commit(empty + s);
@@ -580,6 +600,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           for (int i = 0; i < 16; i++) atomicAdd(dst + i, v[i]);
         }
       }
+    }
+    if (with_db) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)g.db_col, v);
+      if (co < g.cout) atomicAdd(db + co, v[0]);
     }
   }
 
@@ -760,8 +785,8 @@ bool nn_wgrad_tc_supported(int H, int W, int cin, int cout) {
   return nn_conv_tc_supported(H, W, cin, cin) && cout >= 16 && cout % 16 == 0 && cout <= 128 && cin <= 128;
 }
 
-cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, int W, int cin, int cout, int sms,
-                        cudaStream_t s) {
+cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, float* db, int N, int H, int W, int cin, int cout,
+                        int sms, cudaStream_t s) {
   if (!nn_wgrad_tc_supported(H, W, cin, cout)) return cudaErrorNotSupported;
   if ((reinterpret_cast<uintptr_t>(x) & 15) || (reinterpret_cast<uintptr_t>(dy) & 15)) return cudaErrorMisalignedAddress;
   TcWgradGeom g;
@@ -787,18 +812,22 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   // TMEM columns), then the most taps per k-block (9, 3 or 1: one dy tile for
   // kt x tiles), with at least two stages in the CTA's share of the SM's
   // 228 KiB of shared memory.
+  // with db, 32 more TMEM columns (the bias gradient's accumulator); the
+  // 4 KiB block of ones (aligned to 1 KiB) always sits before the barriers
+  const int db_cols = db ? 32 : 0;
+  const size_t extra = 1024 + 4096;
   int cps = 0;
   for (int c = 3; c >= 1 && !cps; c--) {
     const size_t budget = (size_t)228 * 1024 / c - 1024;
     for (int taps = 9; taps >= 3 && !cps; taps /= 3) {
-      if (taps * g.col_stride > 512) continue;
+      if (taps * g.col_stride + db_cols > 512) continue;
       int cols = 32;
-      while (cols < taps * g.col_stride) cols <<= 1;
+      while (cols < taps * g.col_stride + db_cols) cols <<= 1;
       if (c * cols > 512) continue;
       for (int kt = taps; kt >= 1 && !cps; kt /= 3) {
         int st = 4;
-        while (st > 2 && 1024 + (size_t)st * stage_of(kt) + tail_of(kt) + 128 > budget) st--;
-        if (1024 + (size_t)st * stage_of(kt) + tail_of(kt) + 128 > budget) continue;
+        while (st > 2 && 1024 + (size_t)st * stage_of(kt) + tail_of(kt) + extra + 128 > budget) st--;
+        if (1024 + (size_t)st * stage_of(kt) + tail_of(kt) + extra + 128 > budget) continue;
         cps = c;
         g.taps = taps;
         g.ncols = cols;
@@ -810,7 +839,9 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   if (!cps) return cudaErrorNotSupported;
   g.stage_bytes = stage_of(g.kt);
   g.tail = tail_of(g.kt);
-  size_t smem = 1024 + (size_t)g.stages * g.stage_bytes + g.tail + 128;
+  g.db_col = db ? g.taps * g.col_stride : -1;
+  // the ones start at the next 1 KiB after the stages and the tail; the barriers 4 KiB later
+  size_t smem = 1024 + ((size_t)g.stages * g.stage_bytes + g.tail + 1023) / 1024 * 1024 + 4096 + 128;
   // at most cps CTAs on an SM (each holds TMEM): more than 1/(cps+1) of its shared memory each
   const size_t floor_smem = (size_t)228 * 1024 / (cps + 1) + 1;
   if (smem < floor_smem) smem = floor_smem;
@@ -828,13 +859,13 @@ cudaError_t nn_wgrad_tc(const void* x, const void* dy, float* dw, int N, int H, 
   const cuuint32_t xb[4] = {(cuuint32_t)g.MB, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
   const cuuint64_t dd[4] = {(cuuint64_t)cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
   const cuuint64_t ds[3] = {(cuuint64_t)cout * 2, (cuuint64_t)W * cout * 2, (cuuint64_t)H * W * cout * 2};
-  const cuuint32_t db[4] = {(cuuint32_t)g.MA, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
+  const cuuint32_t dyb[4] = {(cuuint32_t)g.MA, (cuuint32_t)g.TW, (cuuint32_t)g.R, 1};
   cudaError_t e = make_map(&xm, x, 4, xd, xs, xb, g.MB * 2);
-  if (e == cudaSuccess) e = make_map(&dm, dy, 4, dd, ds, db, g.MA * 2);
+  if (e == cudaSuccess) e = make_map(&dm, dy, 4, dd, ds, dyb, g.MA * 2);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_wgrad_tc<<<dim3(ctas_x, groups), kTcThreads, smem, s>>>(xm, dm, dw, g);
+  k_wgrad_tc<<<dim3(ctas_x, groups), kTcThreads, smem, s>>>(xm, dm, dw, db, g);
   return cudaGetLastError();
 }
 
