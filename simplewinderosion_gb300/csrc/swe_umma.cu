@@ -5,13 +5,18 @@
 //
 //   k_conv_tc   3x3 convolution, zero padding, NHWC bf16, as an implicit
 //               GEMM: rows = 128-pixel tiles of the output (taken two at a
-//               time), columns = output channels, K = 9 taps x input
-//               channels. Persistent: up to three CTAs per SM stride over
-//               the tile pairs. Per k-block (one tap, KC = 64, 32 or 16
-//               input channels) the TMA loads the tap-shifted 128-pixel tile
-//               of the input straight from the NHWC tensor (pixels beyond
-//               the map edge arrive as zeros: the padding costs nothing) and
-//               the weight slice straight from the [n][tap][k] weights. One
+//               time: a unit), columns = output channels, K = 9 taps x
+//               input channels. Persistent: up to three CTAs per SM stride
+//               over the units. The TMA loads the inputs straight from the
+//               NHWC tensor (pixels beyond the map edge arrive as zeros: the
+//               padding costs nothing) and the weight slices straight from
+//               the [n][tap][k] weights, in one of two schemes: a unit of
+//               two vertically adjacent tiles takes per k-block (dx, KC =
+//               64, 32 or 16 input channels) one box of the dx-shifted input
+//               covering its rows and one row above and below, which the
+//               three dy taps read at offsets of whole image rows; a unit of
+//               two consecutive tiles takes per k-block (tap, KC channels)
+//               one tap-shifted box per tile. One
 //               thread issues the copies, one the MMAs into one of two TMEM
 //               accumulator sets; four warps run the epilogue of the other
 //               set (TMEM -> registers, + bias, optional fused GELU, bf16
@@ -27,7 +32,8 @@
 //               MN-major in the canonical swizzled layout: a TMA box of MA
 //               channels x the tile's 128 pixels, the next MA channels one
 //               box further on; one dy tile per k-block serves up to nine
-//               tap-shifted x tiles.
+//               tap-shifted x tiles. The bias gradient rides along (dy
+//               against a block of ones in shared memory).
 //
 // Every wait on an mbarrier is bounded (2 s by the global timer): past it the
 // kernel records an error code in g_tc_error, stops issuing work, waits
@@ -241,7 +247,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Persistent: each CTA takes units (pairs of M tiles) blockIdx.x,
+// Persistent: each CTA takes units (two M tiles each) blockIdx.x,
 // blockIdx.x + gridDim.x, ...; the copies and MMAs run ahead through the
 // units' k-blocks in one stage ring while the epilogue warps drain the
 // previous unit's accumulators from the other TMEM set.
