@@ -290,6 +290,19 @@ struct Particle {
   float px, py, pz, vx, vy, vz;
 };
 
+// The turbulence draws of a particle's next step (wind.hpp:102-104): keyed
+// by (particle, age after the step's increment, cycle), each an integer in
+// [0, 1000] as a float. They depend on no height, so a caller may take them
+// before the step's heights arrive.
+struct Turbulence {
+  float rx, ry, rz;
+};
+__device__ __forceinline__ Turbulence turbulence(const Particle& p, uint32_t c_lo, uint32_t c_hi, uint32_t seed_lo,
+                                                 uint32_t seed_hi) {
+  const uint4 u = philox4x32((uint32_t)p.id, (uint32_t)(p.age + 1), c_lo, c_hi, seed_lo, seed_hi);
+  return Turbulence{(float)(int)(u.x % 1001u), (float)(int)(u.y % 1001u), (float)(int)(u.z % 1001u)};
+}
+
 // The cell a particle is over (its position rounded, as ivec2(round(...)),
 // wind.hpp:30), or -1 off the map.
 __device__ __forceinline__ long particle_cell(const Consts& c, const Particle& p, int& ix, int& iz) {
@@ -309,8 +322,7 @@ __device__ __forceinline__ long particle_cell(const Consts& c, const Particle& p
 // particle that dies returns -1 and writes nothing (its sediment is exported).
 __device__ __forceinline__ long fly_from(const Consts& c, const ParallelBuffers& B, int32_t* dq, long ci, int ix,
                                          int iz, int32_t q11, int32_t q01, int32_t q21, int32_t q10, int32_t q12,
-                                         uint32_t c_lo, uint32_t c_hi, uint32_t seed_lo, uint32_t seed_hi,
-                                         Particle& p, unsigned& status) {
+                                         const Turbulence& tb, Particle& p, unsigned& status) {
   const int nx = c.nx, nz = c.nz;
   const float inv = c.inv_scale;
   const float sed = fx2f(p.sed_q, inv);
@@ -347,9 +359,7 @@ __device__ __forceinline__ long fly_from(const Consts& c, const ParallelBuffers&
   const V3 rs = cross(n, cross(smul(1.0f - collision, sp), n));
   sp = add(sp, smul(0.9f, sub(smul(shadow, mix(ps, rs, shadow * hfac)), sp)));
   // turbulence draws keyed by (particle, age after this step's increment)
-  const uint4 u = philox4x32((uint32_t)p.id, (uint32_t)p.age, c_lo, c_hi, seed_lo, seed_hi);
-  const float rx = (float)(int)(u.x % 1001u), ry = (float)(int)(u.y % 1001u), rz = (float)(int)(u.z % 1001u);
-  sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(rx, ry, rz), 500.0f)), 500.0f));
+  sp = add(sp, divs(smul(0.1f * hfac * collision, subs(v3(tb.rx, tb.ry, tb.rz), 500.0f)), 500.0f));
   const float drag = 1.0f - 0.3f * sed;
   sp = v3(sp.x * drag, sp.y * drag, sp.z * drag);
   const float npx = p.px + sp.x, npy = py + sp.y, npz = p.pz + sp.z;
@@ -391,7 +401,8 @@ __device__ __forceinline__ long fly_particle(const Consts& c, const ParallelBuff
   const int32_t q21 = H[ix + 1 < c.nx ? ci + nz : ci];
   const int32_t q10 = H[iz > 0 ? ci - 1 : ci];
   const int32_t q12 = H[iz + 1 < nz ? ci + 1 : ci];
-  return fly_from(c, B, B.dq, ci, ix, iz, q11, q01, q21, q10, q12, c_lo, c_hi, seed_lo, seed_hi, p, status);
+  const Turbulence tb = turbulence(p, c_lo, c_hi, seed_lo, seed_hi);
+  return fly_from(c, B, B.dq, ci, ix, iz, q11, q01, q21, q10, q12, tb, p, status);
 }
 
 // Fly phase of one step: Wind::fly for every particle in flight against the
@@ -1275,6 +1286,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       }
       const unsigned pbase = 16u * step;  // tag base of the previous step
       unsigned long long t_wait = 0;
+      Turbulence tb{0.0f, 0.0f, 0.0f};
       for (bool first = true;; first = false) {
         // five loads every pass (rows off the map read the cell's own row;
         // columns off the map land in the padding word or the next row)
@@ -1283,6 +1295,8 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
 #pragma unroll
           for (int q = 0; q < 5; q++) wd[q] = ld_relaxed64(HW + ci + ((need >> q) & 1u ? nbr[q] : 0));
         }
+        // the step's turbulence draws need no height: taken while the loads fly
+        if (first && ci >= 0) tb = turbulence(p, c_lo, c_hi, A.seed_lo, A.seed_hi);
         if (first && check && ci >= 0) {
           prev = pb.bits() & inm;
 #pragma unroll
@@ -1322,8 +1336,7 @@ __device__ __forceinline__ void lanes_cycle(const CycleArgs& A, int slots, int32
       }
       if ((live >> s) & 1u) {
         if (ci >= 0 && !gave_up)
-          ci = fly_from(c, B, dq, ci, ix, iz, hv[0], hv[1], hv[2], hv[3], hv[4], c_lo, c_hi, A.seed_lo, A.seed_hi,
-                        p, status);
+          ci = fly_from(c, B, dq, ci, ix, iz, hv[0], hv[1], hv[2], hv[3], hv[4], tb, p, status);
         else
           ci = -1;
         if (ci >= 0) {
