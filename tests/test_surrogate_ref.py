@@ -68,3 +68,21 @@ def test_network_gradients_by_finite_differences():
                 arr[idx] = old
                 fd = (lp - lm) / (2 * eps)
                 assert abs(fd - grad[idx]) <= 2e-2 * max(1.0, abs(fd)), (name, k, idx, fd, grad[idx])
+
+
+def test_centred_input_moves_each_map_to_the_reference_level():
+    """pack_input with ref (swe_nn_pack_input_centered's restatement): each
+    map's height channel has mean (ref - 0.25) * 4, and a terrain and the
+    same terrain lowered by a constant pack alike (to float rounding)."""
+    rs = np.random.RandomState(4)
+    h = rs.uniform(0.0, 0.6, (3, 16, 12)).astype(np.float32)
+    wind = np.asarray([[0.6, 0.8], [-1.0, 0.0], [0.0, 1.0]], np.float32)
+    x = R.pack_input(h, wind, ref=0.35)
+    means = x[..., 0].reshape(3, -1).astype(np.float64).mean(axis=1)
+    assert np.allclose(means, (0.35 - 0.25) * 4.0, atol=1e-6)
+    y = R.pack_input((h - np.float32(2.5)).astype(np.float32), wind, ref=0.35)
+    assert np.allclose(x[..., 0], y[..., 0], atol=1e-5)
+    assert np.array_equal(x[..., 1:], y[..., 1:])
+    # without ref the packing is the plain affine map
+    z = R.pack_input(h, wind)
+    assert np.array_equal(z[..., 0], (h - np.float32(0.25)) * np.float32(4.0))
