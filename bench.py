@@ -383,6 +383,7 @@ def run_ours(args):
     total_ms = 0.0
     fly_ms = cas_ms = 0.0
     psteps = transfers = 0
+    phases = {}  # the bounded-lanes kernel's own per-step timers, summed over the timed cycles
     for _ in range(args.steps):
         # every timed cycle is a first cycle on the initial terrain, the work
         # the CPU samples time (uploaded outside the timed region)
@@ -399,6 +400,8 @@ def run_ours(args):
         f, c = w.kernel_times()
         fly_ms += f
         cas_ms += c
+        for key, val in w.phase_times().items():
+            phases[key] = phases.get(key, 0.0) + val
         s, _, t = w.stats()
         psteps += s
         transfers += t
@@ -457,7 +460,8 @@ def run_ours(args):
         "kernels": {"cycle_ms": ms_per_step, "fly_phases_ms": fly_ms / args.steps,
                     "cascade_phases_ms": cas_ms / args.steps, "k_transfers_per_step": k,
                     "particle_steps_per_cycle": psteps_per_launch,
-                    "steps_per_particle": psteps_per_launch / particles},
+                    "steps_per_particle": psteps_per_launch / particles,
+                    "step_parts_ms": step_parts(phases, args.steps)},
         "timed_cycles": "each a first cycle on the initial terrain (re-uploaded before it, outside the timing)",
         "roofline": {
             "bound": "hbm",
@@ -578,6 +582,22 @@ def surrogate_leg(swe, torch, dev, h, wind, args):
         "checkpoint": {k: meta[k] for k in ("train_runs", "steps", "batch", "crop", "surrogate_rel_rmse",
                                             "no_change_rel_rmse", "plain_seed_floor_rel_rmse") if k in meta},
     }
+
+
+def step_parts(phases: dict, cycles: int) -> dict | None:
+    """The bounded-lanes kernel's per-cycle split (ms, thread 0 of CTA 0's
+    clock; swe_world_phase_times): the flights' tag waits, the flights
+    themselves, the step's barrier, refills and absorbs, cascades. None for
+    the all-at-once kernel, whose slots hold its colour phases."""
+    if not phases or cycles < 1:
+        return None
+    g = {k: v / cycles for k, v in phases.items()}
+    if g.get("colour2", 0.0) > 0.0:
+        return None
+    fly, tags, barrier = g.get("fly", 0.0), g.get("spawn", 0.0), g.get("unused", 0.0)
+    casc, absorb = g.get("colour0", 0.0), g.get("colour1", 0.0)
+    return {"tag_waits": tags, "flights": fly - tags - barrier, "barrier": barrier, "refill_absorb": absorb,
+            "cascades": casc - absorb}
 
 
 def other_lanes(swe, torch, dev, h, wind, particles, args, world_size, rank, lanes, note):

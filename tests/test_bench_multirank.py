@@ -55,3 +55,17 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     args = bench.parse_args()
     bench.run_reference(args)
     assert capsys.readouterr().out == ""
+
+
+def test_step_parts_split_the_kernel_timers():
+    """The bench line's per-step split of the bounded-lanes kernel: the
+    flights' tag waits and the barrier are parts of the fly slot, the
+    refills and absorbs a part of the cascade slot; the all-at-once kernel
+    (colour phases) gives none."""
+    phases = {"spawn": 300.0, "fly": 1500.0, "unused": 900.0, "colour0": 700.0, "colour1": 150.0,
+              "colour2": 0.0, "ema": 0.0}
+    parts = bench.step_parts(phases, 2)
+    assert parts == {"tag_waits": 150.0, "flights": 150.0, "barrier": 450.0, "refill_absorb": 75.0,
+                     "cascades": 275.0}
+    assert bench.step_parts({}, 2) is None
+    assert bench.step_parts({"fly": 1.0, "colour2": 3.0}, 1) is None
