@@ -111,6 +111,15 @@ def test_surrogate_entry_points_reject_bad_arguments(lib_built):
     L.swe_nn_adam.argtypes = [P, P, P, P, P, ctypes.c_int64] + [ctypes.c_float] * 4 + [ctypes.c_int, P]
     assert L.swe_nn_adam(fake, fake, fake, fake, None, 8, 1e-3, 0.9, 0.999, 1e-8, 0, None) == -1  # step 0
     assert b"adam" in L.swe_last_error()
+    L.swe_nn_pack_input_centered.argtypes = [P, P, P, P] + [ctypes.c_int] * 3 + [ctypes.c_float, P]
+    assert L.swe_nn_pack_input_centered(fake, fake, None, fake, 1, 8, 8, 0.35, None) == -1   # NULL means
+    assert L.swe_nn_pack_input_centered(fake, fake, fake, fake, 0, 8, 8, 0.35, None) == -1   # no maps
+    assert L.swe_nn_pack_input_centered(fake, fake, fake, fake, 1, 8, 8, float("nan"), None) == -1  # NaN ref
+    assert b"pack_input_centered" in L.swe_last_error()
+    L.swe_nn_conv3x3_tc.argtypes = [P, P, P, P, P] + [ctypes.c_int] * 5 + [P]
+    assert L.swe_nn_conv3x3_tc(fake, fake, None, fake, None, 1, 8, 8, 12, 16, None) == -1     # cin % 16
+    L.swe_nn_conv3x3_wgrad_tc.argtypes = [P, P, P, P] + [ctypes.c_int] * 5 + [P]
+    assert L.swe_nn_conv3x3_wgrad_tc(fake, fake, fake, None, 1, 8, 8, 16, 144, None) == -1  # cout > 128
 
 
 def test_surrogate_flop_count():
