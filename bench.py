@@ -63,11 +63,15 @@ def parse_args():
                     help="particles in flight: 0 = default (cells/256, min 1024), -1 = all at once")
     ap.add_argument("--no-all-at-once", action="store_true")
     ap.add_argument("--no-tc", action="store_true", help="surrogate-step: the warp-level mma.sync convolutions")
-    ap.add_argument("--workload", choices=["plain1024", "ensemble", "exact-ensemble", "surrogate", "surrogate-step"],
+    ap.add_argument("--workload", choices=["plain1024", "ensemble", "exact-ensemble", "surrogate", "surrogate-step",
+                                           "longrun"],
                     default="plain1024",
                     help="plain1024: the headline; ensemble: 64 terrains in one persistent launch; "
                          "exact-ensemble: independent 256^2 worlds in ORDERED mode, one thread each; "
-                         "surrogate: train the learned surrogate at 256^2 and measure it against the plain method")
+                         "surrogate: train the learned surrogate at 256^2 and measure it against the plain method; "
+                         "longrun: the surrogate-accelerated large map (--long-size, --long-jumps) against plain-only")
+    ap.add_argument("--long-size", type=int, default=4096, help="longrun: map side")
+    ap.add_argument("--long-jumps", type=int, default=4, help="longrun: 50-cycle jumps (every 4th by the plain method)")
     ap.add_argument("--terrains", type=int, default=64, help="ensemble: number of terrains")
     ap.add_argument("--worlds", type=int, default=8192, help="exact-ensemble: number of worlds")
     ap.add_argument("--pairs", type=int, default=1024, help="surrogate: training pairs")
@@ -1086,6 +1090,48 @@ def run_surrogate(args):
     print(json.dumps(line), flush=True)
 
 
+def run_longrun(args):
+    """The large-domain long run (simplewinderosion_gb300/longrun.py) with the
+    committed checkpoint: `--long-jumps` 50-cycle jumps of a `--long-size`^2
+    map, surrogate jumps in 256^2 tiles with 32-cell halos, every 4th jump by
+    the plain method at one particle per cell per cycle, beside a plain-only
+    run of the same terrain and wind. One JSON line: cycles/s of the
+    accelerated run (host copies of the tiled prediction included) and of
+    the plain-only run, and the comparison after the last judged jump."""
+    import torch
+
+    from simplewinderosion_gb300.longrun import long_run
+    from simplewinderosion_gb300.surrogate import Surrogate
+    from simplewinderosion_gb300.train_surrogate import DEFAULT_OUT
+
+    torch.cuda.set_device(0)
+    with np.load(DEFAULT_OUT) as z:
+        state = {k: z[k] for k in z.files if k != "meta"}
+    model = Surrogate()
+    model.load(state)
+    rec = long_run(model, args.long_size, args.long_jumps, 4, log=lambda *_: None)
+    cycles = rec["jump_cycles"] * rec["jumps"]
+    acc_s, plain_s = rec["seconds"]["accelerated"], rec["seconds"]["plain_only"]
+    judged = [st for st in rec["steps"] if "rel_rmse" in st]
+    line = {
+        "metric": f"surrogate-accelerated erode cycles/s at {args.long_size}^2 (50-cycle jumps, plain method over "
+                  f"every 4th)",
+        "value": cycles / acc_s if acc_s > 0 else None,
+        "unit": "cycles/s",
+        "higher_is_better": True,
+        "plain_only_cycles_per_s": cycles / plain_s if plain_s > 0 else None,
+        "speedup_vs_plain_only": rec["speedup_vs_plain_only"],
+        "jumps": rec["jumps"],
+        "particles_per_cycle": rec["particles_per_cycle"],
+        "tile": rec["tile"],
+        "halo": rec["halo"],
+        "last_comparison": judged[-1] if judged else None,
+        "data": "synthetic",
+        "steps": rec["steps"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -1098,6 +1144,8 @@ def main():
         run_surrogate(args)
     elif args.workload == "surrogate-step":
         run_surrogate_step(args)
+    elif args.workload == "longrun":
+        run_longrun(args)
     else:
         run_ours(args)
 
