@@ -57,7 +57,7 @@ using bf16 = __nv_bfloat16;
 __device__ unsigned int g_tc_error;  // first failure code of a tensor-core kernel (0: none)
 
 constexpr int kTcThreads = 128;
-constexpr int kTcMTiles = 2;  // 128-pixel M tiles per CTA (they share each weight slice)
+constexpr int kTcMTiles = 2;  // 128-pixel M tiles per unit of work (they share each weight slice)
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
