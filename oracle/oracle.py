@@ -93,6 +93,9 @@ def port_lib():
         L.so_stats.argtypes = [_P, _i64p, _i64p, _i64p]
         L.so_glibc_rand_sequence.argtypes = [ctypes.c_uint32, ctypes.c_int, _P]
         L.so_par_erode.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+        L.so_par_set_spawn_mode.argtypes = [_P, ctypes.c_int]
+        L.so_par_max_move.argtypes = [_P]
+        L.so_par_max_move.restype = ctypes.c_float
         L.so_par_get_heights_q.argtypes = [_P, _P]
         L.so_par_ledger.argtypes = [_P, _i64p, _i64p]
         L.so_philox4x32.argtypes = [ctypes.c_uint32] * 6 + [_P]
@@ -205,6 +208,15 @@ class Port:
         c = ctypes.c_uint64(cycle)
         self.L.so_par_erode(self.w, particles, cycles, ctypes.c_uint64(seed), ctypes.byref(c))
         return c.value
+
+    def par_spawn_mode(self, mode: int) -> None:
+        """Which particles fly together in par_erode: 0 the library's rule,
+        1 lane-own id sequences, 2 a fixed spawn schedule (so_par_set_spawn_mode)."""
+        self.L.so_par_set_spawn_mode(self.w, int(mode))
+
+    def par_max_move(self) -> float:
+        """The last par_erode call's largest one-step move along x or z (cells)."""
+        return float(self.L.so_par_max_move(self.w))
 
     def par_heights_q(self) -> np.ndarray:
         a = np.empty(self.n, dtype=np.int32)

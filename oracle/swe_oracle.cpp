@@ -151,6 +151,11 @@ struct so_world {
   std::vector<int32_t> hq;
   bool hq_valid = false;
   int64_t exported_q = 0;
+  // which particles fly together (so_par_set_spawn_mode): 0 the library's
+  // rule, freed lanes take the next ids; 1 lane k takes ids k, k + L, ...;
+  // 2 a fixed schedule, particle j spawning at step floor(400 j / L)
+  int spawn_mode = 0;
+  float max_move = 0.0f;  // the last so_par_erode call's largest step along x or z (cells)
 
   int rnd() {
     switch (rng) {
@@ -527,6 +532,7 @@ struct ParCtx {
   int64_t* tq[4];
   uint32_t seed_lo, seed_hi, c_lo, c_hi;
   int64_t exported, steps, transfers;
+  float max_move = 0.0f;  // largest |step| of a particle along x or z
 };
 
 // One step of one particle against the step-start heights; true if alive.
@@ -581,6 +587,7 @@ bool par_fly(ParCtx& X, PState& P) {
   const float drag = 1.0f - 0.3f * sed;
   sp = v3(sp.x * drag, sp.y * drag, sp.z * drag);
   const float px = P.px + sp.x, pz = P.pz + sp.z;
+  X.max_move = std::fmax(X.max_move, std::fmax(std::fabs(sp.x), std::fabs(sp.z)));
   py = py + sp.y;
   float force = -dot(normalize(sp), n) * length(sp);
   if (force < 0.0f) force = 0.0f;
@@ -696,6 +703,7 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
   std::vector<int32_t> D(n, 0), C(n, 0);
   std::vector<PState> live, next;
   w->st_steps = w->st_particles = w->st_transfers = 0;
+  w->max_move = 0.0f;
   for (int cyc = 0; cyc < cycles; cyc++) {
     const uint64_t cc = *cycle_counter;
     ParCtx X;
@@ -709,8 +717,10 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
     X.C = C.data();
     live.clear();
     const int lanes = so_par_lanes(w->p.lanes, w->nx, w->nz, particles);
+    const int mode = w->spawn_mode;
     int next_id = 0;
-    auto spawn = [&](int i) {
+    std::vector<int> lane_of, next_lane, lane_next(lanes);
+    auto spawn = [&](int i, int lane) {
       uint32_t u[4];
       so_philox4x32((uint32_t)i, 0xFFFFFFFFu, X.c_lo, X.c_hi, X.seed_lo, X.seed_hi, u);
       const int x = (int)(u[0] % (uint32_t)w->nx), z = (int)(u[1] % (uint32_t)w->nz);
@@ -720,14 +730,44 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
       P.px = (float)x + (float)fxq / 1000.0f; P.py = 0.0f; P.pz = (float)z + (float)fzq / 1000.0f;
       P.vx = P.vy = P.vz = 0.0f;
       live.push_back(P);
+      lane_of.push_back(lane);
     };
-    while (next_id < particles && (int)live.size() < lanes) spawn(next_id++);
-    while (!live.empty()) {
+    // the fixed schedule's spawns up to step s: ids j with 400 j < (s + 1) L
+    constexpr long kLife = 400;
+    auto spawn_scheduled = [&](long s) {
+      while (next_id < particles && (long)next_id * kLife < (s + 1) * (long)lanes) {
+        spawn(next_id, 0);
+        next_id++;
+      }
+    };
+    if (mode == 2) {
+      spawn_scheduled(0);
+    } else if (mode == 1) {
+      for (int k = 0; k < lanes && k < particles; k++) {
+        spawn(k, k);
+        lane_next[k] = k + lanes;
+      }
+    } else {
+      while (next_id < particles && (int)live.size() < lanes) {
+        spawn(next_id, (int)live.size());
+        next_id++;
+      }
+    }
+    long step = 0;
+    while (!live.empty() || (mode == 2 && next_id < particles)) {
       X.H = w->hq.data();
       next.clear();
-      for (PState& P : live) {
-        if (par_fly(X, P)) next.push_back(P);
-        else X.exported += P.sed_q;
+      next_lane.clear();
+      std::vector<int> freed;
+      for (size_t q = 0; q < live.size(); q++) {
+        PState& P = live[q];
+        if (par_fly(X, P)) {
+          next.push_back(P);
+          next_lane.push_back(lane_of[q]);
+        } else {
+          X.exported += P.sed_q;
+          freed.push_back(lane_of[q]);
+        }
       }
       if (!next.empty()) {
         int32_t* H = w->hq.data();
@@ -738,8 +778,24 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
         X.transfers += cascade_phase(w, H, C.data());
       }
       live.swap(next);
-      // freed lanes take the cycle's next particles; they fly from the next step
-      while (next_id < particles && (int)live.size() < lanes) spawn(next_id++);
+      lane_of.swap(next_lane);
+      step++;
+      // the particles of the next step: they fly from the next step
+      if (mode == 2) {
+        spawn_scheduled(step);
+      } else if (mode == 1) {
+        for (int lane : freed)
+          if (lane_next[lane] < particles) {
+            spawn(lane_next[lane], lane);
+            lane_next[lane] += lanes;
+          }
+      } else {
+        for (int lane : freed)
+          if (next_id < particles) {
+            spawn(next_id, lane);
+            next_id++;
+          }
+      }
     }
     for (size_t i = 0; i < n; i++) {
       for (int k = 0; k < 4; k++) {
@@ -750,12 +806,17 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
       w->f[0][i] = (float)w->hq[i] * inv;
     }
     w->exported_q += X.exported;
+    w->max_move = std::fmax(w->max_move, X.max_move);
     w->st_steps += X.steps;
     w->st_particles += particles;
     w->st_transfers += X.transfers;
     *cycle_counter = cc + 1;
   }
 }
+
+void so_par_set_spawn_mode(so_world* w, int mode) { w->spawn_mode = mode < 0 || mode > 2 ? 0 : mode; }
+
+float so_par_max_move(so_world* w) { return w->max_move; }
 
 void so_par_get_heights_q(so_world* w, int32_t* dst) {
   ensure_fixed(w);

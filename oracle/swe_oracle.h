@@ -68,6 +68,15 @@ void so_glibc_rand_sequence(uint32_t seed, int n, int32_t* out);
 /* --- CPU model of the parallel fixed-point mode (bitwise model of the GPU
  *     kernels: same float operation order, same counter-based RNG). --- */
 void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_t* cycle_counter);
+// Which particles of a cycle fly together in so_par_erode (default 0): 0 the
+// library's rule (freed lanes take the cycle's next ids); 1 lane k takes ids
+// k, k + L, k + 2L, ...; 2 a fixed schedule, particle j spawning at step
+// floor(400 j / L) (L in flight on average). Modes 1 and 2 are explorations
+// for a parallel mode without a global step barrier; the library runs mode 0.
+void so_par_set_spawn_mode(so_world* w, int mode);
+// The last so_par_erode call's largest one-step move of a particle along x or
+// z, in cells (the reach a cell's visitors can come from).
+float so_par_max_move(so_world* w);
 /* Particles in flight at once: lanes > 0 as given, 0 -> max(1024, cells/256),
  * < 0 -> all particles of the cycle; never more than the cycle's particles. */
 int so_par_lanes(int lanes, int nx, int nz, int particles);

@@ -86,3 +86,26 @@ def test_parallel_model_single_particle_matches_sequential_fly():
     q = p.par_heights_q()
     m, e = p.par_ledger()
     assert int(q.astype(np.int64).sum()) == m
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_refill_variants_conserve_mass_and_differ_only_in_who_flies_together(mode):
+    """The model's refill variants (own id sequences; a fixed spawn schedule):
+    exact conservation, determinism, every particle flown, and a different
+    grouping of particles than the library's rule (so_par_set_spawn_mode);
+    the largest one-step move stays under one cell for normalize(1,0,1)."""
+    a, _ = _world(48, 5, frac_bits=16, lanes=128)
+    b, _ = _world(48, 5, frac_bits=16, lanes=128)
+    base, _ = _world(48, 5, frac_bits=16, lanes=128)
+    a.par_spawn_mode(mode)
+    b.par_spawn_mode(mode)
+    m0, _ = a.par_ledger()
+    for p in (a, b, base):
+        p.par_erode(2000, 2, seed=7)
+    m, e = a.par_ledger()
+    assert m + e == m0
+    steps, spawned, _ = a.stats()
+    assert spawned == 2 * 2000 and steps > 2 * 2000
+    assert np.array_equal(a.par_heights_q(), b.par_heights_q())
+    assert not np.array_equal(a.par_heights_q(), base.par_heights_q())
+    assert 0.0 < a.par_max_move() < 1.0
