@@ -754,11 +754,12 @@ void so_par_erode(so_world* w, int particles, int cycles, uint64_t seed, uint64_
       }
     }
     long step = 0;
+    std::vector<int> freed;
     while (!live.empty() || (mode == 2 && next_id < particles)) {
       X.H = w->hq.data();
       next.clear();
       next_lane.clear();
-      std::vector<int> freed;
+      freed.clear();
       for (size_t q = 0; q < live.size(); q++) {
         PState& P = live[q];
         if (par_fly(X, P)) {
