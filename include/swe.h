@@ -393,8 +393,10 @@ int swe_erode_parallel_noalloc(float* const* fields, int nx, int nz, const swe_p
 int swe_nn_conv3x3(const void* x, const void* w, const float* bias, void* y, int n, int h, int wd, int cin, int cout,
                    void* stream);
 /* The same convolution on the Blackwell tensor cores (tcgen05.mma, fp32
- * accumulators in tensor memory, TMA-fed operand tiles, a 4-stage mbarrier
- * pipeline). Weights come packed by swe_nn_conv3x3_tc_pack: flip == 0 packs
+ * accumulators in tensor memory, TMA-fed operand tiles; a persistent kernel
+ * of up to three CTAs per SM, each a copy/MMA pipeline of up to six
+ * mbarrier stages, the epilogue of one pair of 128-pixel tiles under the
+ * MMAs of the next). Weights come packed by swe_nn_conv3x3_tc_pack: flip == 0 packs
  * w bf16 [cout,3,3,cin] for the forward convolution (x has cin channels, y
  * cout); flip != 0 packs the flipped, transposed weights whose convolution
  * of dy (cout channels) is the input gradient (cin channels), i.e. this call

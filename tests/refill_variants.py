@@ -8,6 +8,11 @@ and the largest one-step move of any particle along x or z (the reach from
 which a cell's visitors come).
 
     python -m tests.refill_variants [N] [P] [C]
+    python -m tests.refill_variants --fixture stats_1024_plain [SEEDS]   # 1024^2, minutes per run
+
+The second form takes the reference's statistics from the committed fixture
+of compiled-reference runs (the benchmark configuration) instead of running
+the reference semantics here.
 
 Prints, per variant and model seed, the worst cycle's 1-Wasserstein
 distance of the height histograms, log-spectrum distance and mean-height
@@ -25,14 +30,25 @@ from tests.statistics_check import floors, reference_summaries
 
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
-    n = int(argv[0]) if len(argv) > 0 else 256
-    particles = int(argv[1]) if len(argv) > 1 else 16384
-    cycles = int(argv[2]) if len(argv) > 2 else 10
     from oracle import oracle
-    h, prof, spec, mean = reference_summaries(n, particles, cycles)
+    if argv[:1] == ["--fixture"]:
+        from simplewinderosion_gb300 import terrain
+        from tests.conftest import golden
+        fx = golden(argv[1])
+        n, particles, cycles = int(fx["n"]), int(fx["particles"]), int(fx["cycles"])
+        h = terrain.config_plain_large(seed=int(fx["terrain_seed"]), n=n)
+        prof, spec, mean = fx["profile"], fx["logspec"], fx["mean"]
+        modes = (0, 2)
+        seeds = tuple(int(v) for v in argv[2].split(",")) if len(argv) > 2 else (5,)
+    else:
+        n = int(argv[0]) if len(argv) > 0 else 256
+        particles = int(argv[1]) if len(argv) > 1 else 16384
+        cycles = int(argv[2]) if len(argv) > 2 else 10
+        h, prof, spec, mean = reference_summaries(n, particles, cycles)
+        modes, seeds = (0, 1, 2), (5, 6)
     names = {0: "library rule", 1: "own id sequences", 2: "fixed spawn schedule"}
-    for mode in (0, 1, 2):
-        for seed in (5, 6):
+    for mode in modes:
+        for seed in seeds:
             p = oracle.Port(n, pspeed=WIND_101, frac_bits=16, lanes=0)
             p.par_spawn_mode(mode)
             p.set_field(0, h)
