@@ -6,7 +6,7 @@ the settings it is benchmarked at (tests/test_gpu_statistics_1024.py).
 Workload: the 1024^2 plain-method terrain (terrain.config_plain_large, seed
 2: fBm base frequency 1/256 + 0.1 +- 0.02 sediment + a 0.4/200 pyramid),
 wind normalize(1,0,1), 1,048,576 particles per cycle, CYCLES cycles, once
-per rand() seed (1, 2, 3; the spread of the three runs is the noise floor).
+per rand() seed (1 to 6; the spread of the six runs is the noise floor).
 For every seed and cycle the file keeps the height map's quantile profile,
 log radial spectrum and mean (tests/terrain_stats.py), and a checksum of the
 initial heights.
@@ -33,7 +33,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
 OUT = Path(__file__).resolve().parent / "stats_1024_plain.npz"
-N, P, TERRAIN_SEED, SEEDS = 1024, 1048576, 2, (1, 2, 3)
+N, P, TERRAIN_SEED, SEEDS = 1024, 1048576, 2, (1, 2, 3, 4, 5, 6)
 WIND_101 = (0.70710677, 0.0, 0.70710677)  # glm::normalize(vec3(1,0,1)) in float
 
 

@@ -50,10 +50,12 @@ def reference_summaries(n, particles, cycles):
 
 
 def floors(prof, spec, mean, c):
-    """Noise floor at cycle index c: the largest distance of seeds 2 and 3 from seed 1."""
-    nw = max(ts.w1_profiles(prof[k, c], prof[0, c]) for k in (1, 2))
-    ns = max(ts.spec_dist_logs(spec[k, c], spec[0, c]) for k in (1, 2))
-    nm = max(abs(mean[k, c] - mean[0, c]) for k in (1, 2))
+    """Noise floor at cycle index c: the largest distance of the other
+    reference seeds' runs from the first seed's."""
+    others = range(1, prof.shape[0])
+    nw = max(ts.w1_profiles(prof[k, c], prof[0, c]) for k in others)
+    ns = max(ts.spec_dist_logs(spec[k, c], spec[0, c]) for k in others)
+    nm = max(abs(mean[k, c] - mean[0, c]) for k in others)
     return nw, ns, nm
 
 
